@@ -1,0 +1,331 @@
+"""Benchmark of the GB300 TurtleSort path; prints one JSON line.
+
+Default workload (the headline metric): n = 2^26 int32 keys, uniform over the
+full int32 range, with an int32 index payload (= position); sorted keys/s.
+
+  value   device-resident keys/s: inputs already in HBM, each step restores the
+          unsorted input with a device copy (untimed) and times one
+          turtle_sort_device call with CUDA events on the sorter's stream.
+          The 512 MiB working set (keys + ids) is larger than L2 and the
+          restore copy rewrites it, so every step starts from cold L2.
+  e2e     the same sort through the reference-facing host API
+          (turtle_start + turtle_sync: pinned host buffers, H2D copies,
+          sort, D2H copies), wall clock per step.
+  roofline  two-pass HBM bound: 4 * n * (4 B key + 4 B id) algorithmic bytes
+          per sort over the measured HBM copy bandwidth.
+  cpu_baseline  the oracle port of the reference algorithm on all host cores,
+          plus std::sort (1 thread) and __gnu_parallel::sort on a sample.
+
+`--impl reference` times the reference algorithm's CPU restatement (the
+oracle port; the reference has no CPU implementation of its own and its GPU
+code cannot be built for the Arm GPU host from this image) on the same
+workload, and prints the same JSON shape with "impl": "reference".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+METRIC = "sorted keys/s (64M int32+idx, device-resident)"
+UNIT = "keys/s"
+
+
+def peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def profile_traffic() -> float | None:
+    """DRAM bytes per launch of the persistent kernel from the committed ncu
+    summary (profiles/persistent_sort_traffic.json), if present."""
+    p = ROOT / "profiles" / "persistent_sort_traffic.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["dram_bytes_per_launch_64M_int32_idx"])
+        except Exception:
+            return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks sampled every 200 ms while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, out: Path | None):
+        self.out = out
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.f = open(self.out, "w") if self.out else subprocess.PIPE
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                out = None
+            if self.out:
+                self.f.close()
+                out = self.out.read_text()
+            self.text = out or ""
+
+    def summary(self, device: int = 0) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.text or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9 or not f[0].isdigit() or int(f[0]) != device:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baselines(keys: np.ndarray, idx: np.ndarray, threads: int) -> dict:
+    """The oracle port of the reference algorithm on all cores (full workload),
+    std::sort on one core and __gnu_parallel::sort on all cores (samples)."""
+    import oracle
+    n = keys.size
+    t0 = time.perf_counter()
+    oracle.turtle_sort(keys, idx, leaf_max=8192, threads=threads)
+    t_port = time.perf_counter() - t0
+    ns = min(n, 1 << 23)
+    k1, i1 = keys[:ns].copy(), idx[:ns].copy()
+    t_std = oracle.cpu_sort_seconds(k1, i1, 0, 1)
+    k2, i2 = keys.copy(), idx.copy()
+    t_par = oracle.cpu_sort_seconds(k2, i2, 2, threads)
+    k3, i3 = keys[:ns].copy(), idx[:ns].copy()
+    t_pu = oracle.cpu_sort_seconds(k3, i3, 1, threads)
+    return {
+        "value": n / t_port, "unit": UNIT, "cores": threads, "kind": "port",
+        "sample": f"oracle 3-pivot quicksort restatement on the full {n} int32+idx workload, "
+                  f"{threads} OpenMP threads",
+        "std_sort_1t_keys_per_s": ns / t_std,
+        "std_sort_1t_sample": f"first {ns} elements",
+        "gnu_parallel_sort_keys_per_s": n / t_par,
+        "std_sort_par_unseq_keys_per_s": ns / t_pu,
+        "par_unseq_note": "libstdc++ without TBB runs par_unseq serially",
+        "host_threads": oracle.hardware_threads(),
+    }
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle
+    from turtlesort_gb300 import datagen as dg
+    n = args.n
+    keys, idx = dg.sweep_input("a", n)
+    threads = os.cpu_count() or 1
+    times = []
+    for s in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        oracle.turtle_sort(keys, idx, leaf_max=8192, threads=threads)
+        dt = time.perf_counter() - t0
+        if s >= args.warmup:
+            times.append(dt)
+    tot = sum(times)
+    v = n * len(times) / tot
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (splitmix64, seed 0x7475727432)",
+        "config": {"workload": f"sort n={n} int32 keys uniform full range + int32 index"},
+        "cpu_baseline": {
+            "value": v, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "the reference's 3-pivot quicksort restated in C++ (oracle), full workload "
+                      "per step; the reference has no CPU sort and its CUDA sources are not "
+                      "present on the GPU host"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args) -> None:
+    import torch
+    import turtlesort_gb300 as ts
+    from turtlesort_gb300 import datagen as dg
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_
+        dist_.init_process_group("nccl")
+        dist = dist_
+
+    n = args.n
+    keys, idx = dg.sweep_input("a", n)
+    dev = torch.device("cuda", local)
+    d_src_k = torch.from_numpy(keys).to(dev)
+    d_src_i = torch.from_numpy(idx).to(dev)
+    d_k = torch.empty_like(d_src_k)
+    d_i = torch.empty_like(d_src_i)
+    sorter = ts.TurtleSort(np.int32, n, compress=False, track_index=True, device=local)
+    stream = torch.cuda.Stream(device=dev)
+    sh = stream.cuda_stream
+
+    def one_step(timed: bool):
+        with torch.cuda.stream(stream):
+            d_k.copy_(d_src_k)
+            d_i.copy_(d_src_i)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            sorter.sort_device(d_k.data_ptr(), d_i.data_ptr(), n, sh)
+            e1.record(stream)
+        return e0, e1
+
+    for _ in range(args.warmup):
+        one_step(False)
+    torch.cuda.synchronize()
+    sorter.status(sh)
+    # correctness spot check of the last warm-up result (cheap, untimed)
+    out_k = d_k[: 1 << 16].cpu().numpy()
+    if not np.all(out_k[:-1] <= out_k[1:]):
+        raise RuntimeError("device sort produced unsorted output")
+
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = sorter.launches
+    clocks = ClockSampler(Path(args.clocks_csv) if args.clocks_csv else None)
+    events = []
+    with clocks:
+        t_wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            events.append(one_step(True))
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall0
+    sorter.status(sh)
+    launches = sorter.launches - launches0
+    ms = [a.elapsed_time(b) for a, b in events]
+    tot_ms = sum(ms)
+    if dist is not None:
+        t = torch.tensor([tot_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tot_ms = float(t.item())
+        dist.barrier()
+    ms_step = tot_ms / args.steps
+    value = world * n * args.steps / (tot_ms / 1e3)
+
+    # full check of the final result against the properties of a sort
+    fk = d_k.cpu().numpy()
+    fi = d_i.cpu().numpy()
+    if not (np.all(fk[:-1] <= fk[1:]) and np.array_equal(keys[fi], fk)):
+        raise RuntimeError("final device result is not a sorted permutation")
+
+    # end to end through the reference-facing API with pinned host buffers
+    h_k = torch.empty(n, dtype=torch.int32, pin_memory=True)
+    h_i = torch.empty(n, dtype=torch.int32, pin_memory=True)
+    hk, hi = h_k.numpy(), h_i.numpy()
+    e2e_t = []
+    for s in range(args.warmup + args.steps):
+        hk[:] = keys
+        hi[:] = idx
+        sorter.StartSorting(hk, hi)
+        secs = sorter.Sync()
+        if s >= args.warmup:
+            e2e_t.append(secs)
+    if not np.array_equal(hk, fk):
+        raise RuntimeError("end-to-end result differs from the device result")
+    e2e_value = world * n * len(e2e_t) / sum(e2e_t)
+
+    if rank != 0:
+        return
+    peak, peak_kind = peaks()
+    alg_bytes = 4.0 * n * (4 + 4)
+    achieved = alg_bytes / (ms_step / 1e3) / 1e9
+    traffic = profile_traffic()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (splitmix64 seed 0x7475727432; uniform full int32 range; index = position)",
+        "config": {"workload": f"sort n={n} int32 keys + int32 index (64M, uniform)",
+                   "n": n, "key": "int32", "payload": "int32", "l2": "inputs (512 MiB) larger "
+                   "than L2; each step restores the input with a device copy (untimed)",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": f"{peak_kind} hbm_gbs",
+                     "algorithmic_bytes": alg_bytes,
+                     "kernel": "persistent_sort_kernel<uint32_t,true> (one launch per sort)"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 8,
+                "d2h_bytes_per_step": n * 8,
+                "path": "turtle_start/turtle_sync (StartSorting/Sync) with pinned host buffers"},
+        "gpu_launches": int(launches),
+        "wall_s_timed": t_wall,
+        "levels": sorter.last_levels,
+        "clocks": clocks.summary(local),
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baselines(keys, idx, os.cpu_count() or 1)
+    print(json.dumps(line), flush=True)
+    sorter.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=1 << 26)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--clocks-csv", default=None)
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,161 @@
+/*
+ * turtle_gb300.h -- C ABI of the GB300 (sm_103a) TurtleSort sort path.
+ *
+ * Plain C: no CUDA, C++ or torch types.  Streams are passed as `void*`
+ * (a cudaStream_t; NULL = the handle's own stream).  Every entry point
+ * returns a turtle_status (0 = success) and never exits the process.
+ *
+ * Each declaration names the reference interface it replaces
+ * (tugrul512bit/TurtleSort, file:line).
+ */
+#ifndef TURTLE_GB300_H
+#define TURTLE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Key types.  The reference instantiates its kernels for char, unsigned
+ * char, short, unsigned short, int, unsigned, long, unsigned long
+ * (turtle-sort.cu:956-1134); these are the same eight integer types. */
+typedef enum turtle_dtype {
+  TURTLE_INT8 = 0,
+  TURTLE_UINT8 = 1,
+  TURTLE_INT16 = 2,
+  TURTLE_UINT16 = 3,
+  TURTLE_INT32 = 4,
+  TURTLE_UINT32 = 5,
+  TURTLE_INT64 = 6,
+  TURTLE_UINT64 = 7
+} turtle_dtype;
+
+/* Status codes.  The reference aborts the process on any CUDA error
+ * (turtle-globals.cuh:18-30, gpuErrchk -> exit) and prints device-side errors
+ * (turtle-sort.cu:146,608,859); these codes replace both. */
+typedef enum turtle_status {
+  TURTLE_OK = 0,
+  TURTLE_ERR_INVALID_ARGUMENT = 1, /* null handle/pointer, bad dtype, n < 0 */
+  TURTLE_ERR_TOO_LARGE = 2,        /* n (or arrays x size) above the handle's max_n */
+  TURTLE_ERR_CUDA = 3,             /* a CUDA runtime/driver call failed */
+  TURTLE_ERR_OUT_OF_MEMORY = 4,    /* device or pinned allocation failed */
+  TURTLE_ERR_TIMEOUT = 5,          /* a bounded device-side wait gave up */
+  TURTLE_ERR_CAPACITY = 6,         /* a device work list would have overflowed */
+  TURTLE_ERR_STATE = 7,            /* e.g. Sync without StartSorting */
+  TURTLE_ERR_ALIGNMENT = 8,        /* device pointer not 16-byte aligned */
+  TURTLE_ERR_NO_DEVICE = 9,        /* no usable CUDA device */
+  TURTLE_ERR_BUDGET = 10           /* a request can never fit the HBM budget */
+} turtle_status;
+
+typedef struct turtle_sorter turtle_sorter; /* opaque */
+
+/* ---- the drop-in sorter (turtle-sort.cuh:31-283, struct TurtleSort) ---- */
+
+/* Replaces TurtleSort(int maxElements, bool optInCompression)
+ * (turtle-sort.cuh:63-113): device buffers for up to max_n keys (+ int32
+ * index when track_index != 0), a private stream, and the work lists of the
+ * persistent sort kernel.  Buffers come from the CUDA driver VMM API; with
+ * compress != 0 they request generic compression when the device supports it
+ * (turtle-buffer.cuh:27-70, quick-helper.cuh:57-105).  device < 0 means the
+ * current device (the reference hard-codes device 0, turtle-sort.cuh:73). */
+turtle_status turtle_create(turtle_dtype dtype, int64_t max_n, int track_index, int compress,
+                            int device, turtle_sorter** out);
+
+/* Replaces ~TurtleSort (turtle-sort.cuh:278-282) and the Buffer destructors
+ * (turtle-buffer.cuh:82-99).  Safe on NULL. */
+turtle_status turtle_destroy(turtle_sorter* s);
+
+/* Replaces MemoryCompressionSuccessful() (turtle-sort.cuh:115-118): 1 when
+ * the key buffers really were allocated compressible. */
+int turtle_compression_ok(const turtle_sorter* s);
+
+/* Replaces StartSorting(std::vector<Type>*, std::vector<int>*)
+ * (turtle-sort.cuh:124-184): copies n keys (and n int32 ids when idx is not
+ * NULL) from host memory and starts the sort asynchronously.  The host
+ * buffers must stay valid until turtle_sync returns; results are written back
+ * into them by turtle_sync. */
+turtle_status turtle_start(turtle_sorter* s, void* host_keys, int32_t* host_idx, int64_t n);
+
+/* Replaces double Sync() (turtle-sort.cuh:188-258): waits for the sort,
+ * copies keys (and ids) back into the buffers given to turtle_start and
+ * stores the seconds elapsed since turtle_start in *seconds (may be NULL). */
+turtle_status turtle_sync(turtle_sorter* s, double* seconds);
+
+/* Replaces MultiSort<Type,ArrSize,BlockSize,UseSharedMemory>(numArrays, ptr)
+ * (turtle-sort.cuh:265-276 -> turtle-multi-sort.cuh:195-205): sorts
+ * num_arrays contiguous arrays of arr_size keys in place in host memory,
+ * synchronously.  block_size is accepted for source compatibility and only
+ * checked the way the reference requires (num_arrays % block_size == 0).
+ * num_arrays * arr_size must not exceed max_n.  *seconds (may be NULL)
+ * receives the wall time including both copies, like the reference. */
+turtle_status turtle_multisort(turtle_sorter* s, void* host_keys, int64_t arr_size,
+                               int64_t num_arrays, int block_size, double* seconds);
+
+/* ---- device-resident forms (no reference counterpart; new API) ---- */
+
+/* Sorts n keys (and ids) that are already in device memory, in place, on
+ * `stream` (NULL = the sorter's stream).  Asynchronous: call
+ * turtle_stream_status (or synchronize the stream) before reading results. */
+turtle_status turtle_sort_device(turtle_sorter* s, void* d_keys, int32_t* d_idx, int64_t n,
+                                 void* stream);
+
+/* Batched uneven form: num arrays packed back to back in d_keys (and d_idx),
+ * array i = [offsets[i], offsets[i+1]), offsets in device memory (num + 1
+ * int64 values, offsets[0] = 0, non-decreasing, offsets[num] <= max_n).
+ * All arrays are sorted by one persistent launch; the launch is captured in a
+ * CUDA graph the first time a given (pointers, num, total) is seen and
+ * replayed afterwards.  Asynchronous like turtle_sort_device. */
+turtle_status turtle_sort_batched_device(turtle_sorter* s, void* d_keys, int32_t* d_idx,
+                                         const int64_t* d_offsets, int64_t num, int64_t total,
+                                         void* stream);
+
+/* Fixed-size batched form on device memory: num_arrays arrays of arr_size
+ * keys (one CTA or thread group per array, shared-memory sort).  Arrays
+ * longer than the shared-memory capacity go through the batched persistent
+ * path.  Asynchronous. */
+turtle_status turtle_multisort_device(turtle_sorter* s, void* d_keys, int32_t* d_idx,
+                                      int64_t arr_size, int64_t num_arrays, void* stream);
+
+/* Waits for the work issued on `stream` (NULL = the sorter's stream) and
+ * returns the device-side status of the last sort on this sorter
+ * (TURTLE_OK, TURTLE_ERR_TIMEOUT, TURTLE_ERR_CAPACITY). */
+turtle_status turtle_stream_status(turtle_sorter* s, void* stream);
+
+/* ---- introspection ---- */
+
+/* Kernel launches issued by this sorter since it was created. */
+int64_t turtle_launch_count(const turtle_sorter* s);
+
+/* Partition levels run by the last completed sort (after turtle_stream_status
+ * or turtle_sync). */
+int turtle_last_levels(const turtle_sorter* s);
+
+/* Largest n a sorter of this dtype can be created for (limited by the int32
+ * index payload when track_index != 0). */
+int64_t turtle_max_elements(turtle_dtype dtype, int track_index);
+
+/* Element capacity of the one-CTA shared-memory sort for this dtype: arrays
+ * up to this length are sorted without a partition pass. */
+int64_t turtle_smem_capacity(turtle_dtype dtype, int track_index);
+
+/* Short text for a status code (static storage). */
+const char* turtle_status_string(turtle_status st);
+
+/* Text of the last CUDA error seen by this sorter ("" if none). */
+const char* turtle_last_cuda_error(const turtle_sorter* s);
+
+/* Host-side fault injection for tests: the next `count` device-buffer
+ * allocations fail as if the device were out of memory.  No GPU fault is
+ * involved; callers see TURTLE_ERR_OUT_OF_MEMORY. */
+void turtle_debug_fail_allocations(int count);
+
+/* Library version string (static storage). */
+const char* turtle_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TURTLE_GB300_H */

@@ -1,0 +1,199 @@
+"""Parity of the GB300 sort path against the CPU oracle (runs on a GPU).
+
+Every case goes through the C ABI (via the Python mirror of the reference
+API).  Values must be bit-identical to np.sort / the oracle; the index output
+must equal the oracle's stable order exactly (the GB300 partition and leaf
+sorts are stable, so ties keep their input order), which also proves it is a
+permutation with orig[idx[i]] == out[i].
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import ALL_DTYPES
+from turtlesort_gb300 import TurtleSort, TurtleError, smem_capacity
+from turtlesort_gb300 import datagen as dg
+
+pytestmark = pytest.mark.gpu
+
+_SORTERS: dict = {}
+
+
+def sorter(dtype, track=True, max_n=1 << 21):
+    key = (np.dtype(dtype), track, max_n)
+    if key not in _SORTERS:
+        _SORTERS[key] = TurtleSort(dtype, max_n, compress=False, track_index=track)
+    return _SORTERS[key]
+
+
+def make_keys(dtype, n, dist, seed):
+    lo, hi = dg.dtype_range(dtype)
+    if dist == "uniform":
+        return dg.uniform(dtype, n, seed)
+    if dist == "dups":
+        return dg.uniform(dtype, n, seed, 0, 3)
+    if dist == "equal":
+        return np.full(n, 7 if lo >= 0 else -5, dtype=dtype)
+    if dist == "sorted":
+        return np.sort(dg.uniform(dtype, n, seed))
+    if dist == "reverse":
+        return np.sort(dg.uniform(dtype, n, seed))[::-1].copy()
+    if dist == "organ":
+        s = np.sort(dg.uniform(dtype, n, seed))
+        return np.concatenate([s[0::2], s[1::2][::-1]])[:n].astype(dtype)
+    if dist == "extremes":
+        pool = np.array([lo, hi, 0, 1, hi - 1, lo + 1] + ([-1] if lo < 0 else []), dtype=dtype)
+        pick = (dg.splitmix64(seed, 0, n) % np.uint64(pool.size)).astype(np.int64)
+        return pool[pick]
+    if dist == "two":
+        return np.where(dg.uniform(np.uint8, n, seed) & 1, hi, lo).astype(dtype)
+    raise ValueError(dist)
+
+
+def check_sorted_pair(keys_in, out_k, out_i, idx_in):
+    order = np.argsort(keys_in, kind="stable")
+    exp_k = keys_in[order]
+    assert out_k.dtype == keys_in.dtype
+    bad = np.nonzero(out_k != exp_k)[0]
+    assert bad.size == 0, f"{bad.size} key mismatches, first at {bad[:5]}"
+    if idx_in is not None:
+        exp_i = idx_in[order]
+        badi = np.nonzero(out_i != exp_i)[0]
+        assert badi.size == 0, f"{badi.size} index mismatches, first at {badi[:5]}"
+
+
+def tile(dtype):
+    return smem_capacity(dtype)
+
+
+SIZES_SMALL = [0, 1, 2, 3, 16, 17, 31, 32, 33, 127, 128, 129, 1000]
+
+
+@pytest.mark.parametrize("dtype", ALL_DTYPES)
+@pytest.mark.parametrize("dist", ["uniform", "dups", "equal", "sorted", "reverse", "organ",
+                                  "extremes", "two"])
+def test_start_sync_sizes(dtype, dist):
+    t = tile(dtype)
+    sizes = SIZES_SMALL + [t - 1, t, t + 1, 2 * t + 3, 4 * t - 1, 50_000, 300_001]
+    s = sorter(dtype)
+    for j, n in enumerate(sizes):
+        k = make_keys(dtype, n, dist, 1000 + j)
+        idx = np.arange(n, dtype=np.int32)
+        ko, io = k.copy(), idx.copy()
+        s.StartSorting(ko, io)
+        s.Sync()
+        check_sorted_pair(k, ko, io, idx)
+
+
+@pytest.mark.parametrize("dtype", ALL_DTYPES)
+def test_keys_only(dtype):
+    s = sorter(dtype, track=False)
+    for n in [5, 4096, 70_000, 1_000_000]:
+        k = dg.uniform(dtype, n, 77 + n)
+        ko = k.copy()
+        s.StartSorting(ko)
+        s.Sync()
+        assert np.array_equal(ko, np.sort(k))
+
+
+@pytest.mark.parametrize("dtype", [np.int32, np.uint8, np.int64])
+def test_large_matches_oracle(dtype, oracle_mod):
+    n = 2_000_000
+    s = sorter(dtype)
+    for dist, seed in [("uniform", 1), ("dups", 2), ("sorted", 3)]:
+        k = make_keys(dtype, n, dist, seed)
+        idx = dg.uniform(np.int32, n, seed + 50)  # arbitrary payload
+        ko, io = k.copy(), idx.copy()
+        s.StartSorting(ko, io)
+        s.Sync()
+        ek, ei = oracle_mod.turtle_sort(k, idx, leaf_max=tile(dtype), threads=4)
+        assert np.array_equal(ko, ek)
+        assert np.array_equal(io, ei)
+
+
+def test_index_equals_value_readme_check():
+    # the reference benchmark's own check (README.md:190-209): index
+    # initialised to the value must still equal the value after sorting
+    v, i = dg.plain_sort_input(1 << 20)
+    s = sorter(np.int32)
+    s.StartSorting(v, i)
+    s.Sync()
+    assert np.all(v[:-1] <= v[1:])
+    assert np.array_equal(v, i)
+
+
+def test_device_api_torch():
+    torch = pytest.importorskip("torch")
+    n = 1 << 20
+    k = dg.uniform(np.int32, n, 5)
+    i = np.arange(n, dtype=np.int32)
+    tk = torch.from_numpy(k.copy()).cuda()
+    ti = torch.from_numpy(i.copy()).cuda()
+    s = sorter(np.int32)
+    stream = torch.cuda.current_stream().cuda_stream
+    s.sort_device(tk.data_ptr(), ti.data_ptr(), n, stream)
+    s.status(stream)
+    check_sorted_pair(k, tk.cpu().numpy(), ti.cpu().numpy(), i)
+
+
+@pytest.mark.parametrize("dtype", [np.int32, np.int16, np.uint64])
+def test_batched_uneven(dtype, oracle_mod):
+    torch = pytest.importorskip("torch")
+    num = 3000
+    lens = dg.loguniform_lengths(num, 1, 40000, 11)
+    lens[::97] = 0
+    offs = np.zeros(num + 1, dtype=np.int64)
+    np.cumsum(lens, out=offs[1:])
+    total = int(offs[-1])
+    k = dg.uniform(dtype, total, 12)
+    i = np.arange(total, dtype=np.int32)
+    s = sorter(dtype, max_n=max(total, 1 << 21))
+    tk = torch.from_numpy(k.copy()).cuda()
+    ti = torch.from_numpy(i.copy()).cuda()
+    to = torch.from_numpy(offs).cuda()
+    for rep in range(2):  # second call replays the captured graph
+        tk.copy_(torch.from_numpy(k))
+        ti.copy_(torch.from_numpy(i))
+        s.sort_batched_device(tk.data_ptr(), ti.data_ptr(), to.data_ptr(), num, total)
+        s.status()
+        ek, ei = oracle_mod.segmented_sort(k, offs, i)
+        assert np.array_equal(tk.cpu().numpy(), ek)
+        assert np.array_equal(ti.cpu().numpy(), ei)
+
+
+@pytest.mark.parametrize("dtype", ALL_DTYPES)
+@pytest.mark.parametrize("arr", [1, 2, 10, 16, 17, 32, 100, 1024, 2038])
+def test_multisort_matches_heap_oracle(dtype, arr, oracle_mod):
+    num = 64 * 37
+    s = sorter(dtype, track=False, max_n=1 << 23)
+    k = dg.uniform(dtype, arr * num, 300 + arr)
+    h = k.copy()
+    s.MultiSort(arr, num, h, block_size=64)
+    exp = oracle_mod.multisort_heap(k, arr, num)
+    assert np.array_equal(h, exp)
+
+
+def test_multisort_long_arrays_use_batched_path(oracle_mod):
+    dtype = np.int32
+    arr = tile(dtype) * 3 + 5
+    num = 7
+    s = sorter(dtype, track=False, max_n=1 << 23)
+    k = dg.uniform(dtype, arr * num, 9)
+    h = k.copy()
+    s.MultiSort(arr, num, h, block_size=1)
+    assert np.array_equal(h.reshape(num, arr), np.sort(k.reshape(num, arr), axis=1))
+
+
+def test_errors():
+    s = sorter(np.int32)
+    big = np.zeros(s.max_elements + 1, dtype=np.int32)
+    with pytest.raises(TurtleError) as e:
+        s.StartSorting(big)
+    assert e.value.status == 2  # TURTLE_ERR_TOO_LARGE
+    with pytest.raises(TurtleError) as e:
+        s.Sync()  # no StartSorting pending
+    assert e.value.status == 7
+    h = np.zeros(10 * 33, dtype=np.int32)
+    with pytest.raises(TurtleError):
+        s.MultiSort(10, 33, h, block_size=32)  # 33 % 32 != 0, as the reference requires

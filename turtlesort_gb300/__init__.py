@@ -1,0 +1,181 @@
+"""GB300-native TurtleSort sort path.
+
+Python mirror of the reference host API (turtle-sort.cuh:31-283) over the
+C ABI of libturtle_gb300.so.  The class and method names follow the reference
+so that code and tests read like the reference's own programs::
+
+    sorter = TurtleSort(np.int32, max_elements=n, compress=False)
+    sorter.StartSorting(values, index)   # asynchronous, like the reference
+    seconds = sorter.Sync()              # values/index sorted in place
+    seconds = sorter.MultiSort(arr_size, num_arrays, host_array)
+
+Device-resident forms (no reference counterpart) take raw device pointers
+(e.g. ``tensor.data_ptr()``) and a CUDA stream handle.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import _native
+from ._native import TurtleError
+
+__all__ = ["TurtleSort", "TurtleError", "dtype_code", "smem_capacity", "load_library"]
+
+_DTYPES = {
+    np.dtype(np.int8): _native.INT8,
+    np.dtype(np.uint8): _native.UINT8,
+    np.dtype(np.int16): _native.INT16,
+    np.dtype(np.uint16): _native.UINT16,
+    np.dtype(np.int32): _native.INT32,
+    np.dtype(np.uint32): _native.UINT32,
+    np.dtype(np.int64): _native.INT64,
+    np.dtype(np.uint64): _native.UINT64,
+}
+
+
+def load_library():
+    return _native.load()
+
+
+def dtype_code(dtype) -> int:
+    dt = np.dtype(dtype)
+    if dt not in _DTYPES:
+        raise TypeError(f"unsupported key dtype {dt} (integer types int8..uint64 only)")
+    return _DTYPES[dt]
+
+
+def smem_capacity(dtype, track_index: bool = True) -> int:
+    """Longest array the one-CTA shared-memory sort handles for this dtype."""
+    return int(load_library().turtle_smem_capacity(dtype_code(dtype), int(track_index)))
+
+
+def _check(st: int, where: str, handle=None) -> None:
+    if st != 0:
+        detail = ""
+        if handle is not None:
+            raw = load_library().turtle_last_cuda_error(handle)
+            detail = raw.decode() if raw else ""
+        raise TurtleError(st, where, detail)
+
+
+class TurtleSort:
+    """Mirror of Turtle::TurtleSort<Type, TrackIndex> (turtle-sort.cuh:31-283).
+
+    ``dtype`` is the key type (the reference's template parameter), ``track_index``
+    the TrackIndex template flag, ``max_elements``/``compress`` the constructor
+    arguments (turtle-sort.cuh:63).
+    """
+
+    def __init__(self, dtype, max_elements: int, compress: bool = False,
+                 track_index: bool = True, device: int = -1):
+        self._lib = load_library()
+        self.dtype = np.dtype(dtype)
+        self._code = dtype_code(self.dtype)
+        self.max_elements = int(max_elements)
+        self.track_index = bool(track_index)
+        h = C.c_void_p()
+        _check(self._lib.turtle_create(self._code, self.max_elements, int(track_index),
+                                       int(compress), int(device), C.byref(h)),
+               "TurtleSort()")
+        self._h = h
+        self._pending = None
+
+    # -- lifetime --
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.turtle_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- reference API --
+    def MemoryCompressionSuccessful(self) -> bool:
+        return bool(self._lib.turtle_compression_ok(self._h))
+
+    def StartSorting(self, values: np.ndarray, index: Optional[np.ndarray] = None) -> None:
+        """Starts sorting ``values`` (and reorders ``index`` alongside); returns
+        immediately.  Both arrays are updated in place by :meth:`Sync`."""
+        if values.dtype != self.dtype or not values.flags.c_contiguous:
+            raise TypeError(f"values must be a contiguous {self.dtype} array")
+        if not self.track_index:
+            index = None  # TrackIndex=false ignores the index (turtle-sort.cuh:176-179)
+        if index is not None:
+            if index.dtype != np.int32 or not index.flags.c_contiguous:
+                raise TypeError("index must be a contiguous int32 array")
+            if index.shape[0] != values.shape[0]:
+                raise ValueError("values and index must have the same size")
+        n = int(values.shape[0])
+        st = self._lib.turtle_start(self._h, values.ctypes.data_as(C.c_void_p),
+                                    index.ctypes.data_as(C.c_void_p) if index is not None else None,
+                                    n)
+        _check(st, "StartSorting", self._h)
+        self._pending = (values, index)  # keep the buffers alive until Sync
+
+    def Sync(self) -> float:
+        """Waits for the sort, writes results back; returns elapsed seconds."""
+        secs = C.c_double(0.0)
+        st = self._lib.turtle_sync(self._h, C.byref(secs))
+        self._pending = None
+        _check(st, "Sync", self._h)
+        return float(secs.value)
+
+    def MultiSort(self, arr_size: int, num_arrays: int, host: np.ndarray,
+                  block_size: int = 32) -> float:
+        """Sorts ``num_arrays`` contiguous arrays of ``arr_size`` keys in place
+        (MultiSort<Type, arrSize, blockSize>, turtle-sort.cuh:265-276)."""
+        if host.dtype != self.dtype or not host.flags.c_contiguous:
+            raise TypeError(f"host must be a contiguous {self.dtype} array")
+        if host.size < arr_size * num_arrays:
+            raise ValueError("host array smaller than num_arrays * arr_size")
+        secs = C.c_double(0.0)
+        st = self._lib.turtle_multisort(self._h, host.ctypes.data_as(C.c_void_p), int(arr_size),
+                                        int(num_arrays), int(block_size), C.byref(secs))
+        _check(st, "MultiSort", self._h)
+        return float(secs.value)
+
+    # -- device-resident forms --
+    def sort_device(self, keys_ptr: int, idx_ptr: Optional[int], n: int, stream: int = 0) -> None:
+        st = self._lib.turtle_sort_device(self._h, C.c_void_p(keys_ptr),
+                                          C.c_void_p(idx_ptr) if idx_ptr else None, int(n),
+                                          C.c_void_p(stream) if stream else None)
+        _check(st, "sort_device", self._h)
+
+    def sort_batched_device(self, keys_ptr: int, idx_ptr: Optional[int], offsets_ptr: int,
+                            num: int, total: int, stream: int = 0) -> None:
+        st = self._lib.turtle_sort_batched_device(
+            self._h, C.c_void_p(keys_ptr), C.c_void_p(idx_ptr) if idx_ptr else None,
+            C.c_void_p(offsets_ptr), int(num), int(total), C.c_void_p(stream) if stream else None)
+        _check(st, "sort_batched_device", self._h)
+
+    def multisort_device(self, keys_ptr: int, idx_ptr: Optional[int], arr_size: int,
+                         num_arrays: int, stream: int = 0) -> None:
+        st = self._lib.turtle_multisort_device(
+            self._h, C.c_void_p(keys_ptr), C.c_void_p(idx_ptr) if idx_ptr else None,
+            int(arr_size), int(num_arrays), C.c_void_p(stream) if stream else None)
+        _check(st, "multisort_device", self._h)
+
+    def status(self, stream: int = 0) -> None:
+        """Waits for ``stream`` and raises if the device reported an error."""
+        st = self._lib.turtle_stream_status(self._h, C.c_void_p(stream) if stream else None)
+        _check(st, "device status", self._h)
+
+    @property
+    def launches(self) -> int:
+        return int(self._lib.turtle_launch_count(self._h))
+
+    @property
+    def last_levels(self) -> int:
+        return int(self._lib.turtle_last_levels(self._h))

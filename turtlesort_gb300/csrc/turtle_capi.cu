@@ -1,0 +1,514 @@
+// C ABI of the GB300 TurtleSort path (declared in include/turtle_gb300.h).
+//
+// A turtle_sorter is the GB300 counterpart of Turtle::TurtleSort<T,TrackIndex>
+// (turtle-sort.cuh:31-283): it owns the device buffers (driver VMM memory, see
+// turtle_vmm.cu), a private non-blocking stream, the work lists of the
+// persistent sort kernel and a pinned status block.  Entry points return
+// status codes; nothing calls exit().
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/turtle_gb300.h"
+#include "turtle_device.cuh"
+#include "turtle_internal.h"
+
+using turtle::DevBuffer;
+
+namespace {
+
+struct WsLayout {
+  int segCap = 0, tileCap = 0, leafCap = 0, fillCap = 0;
+  size_t offCtrl = 0, offSegs[2] = {0, 0}, offTileCnt[2] = {0, 0}, offTileOff[2] = {0, 0};
+  size_t offLeaves = 0, offLeavesSorted = 0, offFills = 0, bytes = 0;
+};
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+WsLayout make_layout(long long maxN, int tile, long long extraLeaves) {
+  WsLayout L;
+  const long long segCap = maxN / tile + 66;
+  const long long tileCap = maxN / tile + 2 * segCap + 64;
+  const long long leafCap = 8 * (segCap + 1) + extraLeaves + 1024;
+  const long long fillCap = 2 * (3 * (segCap + 1) + tileCap) + 1024;
+  L.segCap = (int)segCap;
+  L.tileCap = (int)tileCap;
+  L.leafCap = (int)leafCap;
+  L.fillCap = (int)fillCap;
+  size_t o = 0;
+  L.offCtrl = o; o = align_up(o + sizeof(turtle::Control), 256);
+  for (int p = 0; p < 2; ++p) { L.offSegs[p] = o; o = align_up(o + segCap * sizeof(turtle::SegDesc), 256); }
+  for (int p = 0; p < 2; ++p) { L.offTileCnt[p] = o; o = align_up(o + tileCap * 8 * sizeof(int), 256); }
+  for (int p = 0; p < 2; ++p) { L.offTileOff[p] = o; o = align_up(o + tileCap * 8 * sizeof(long long), 256); }
+  L.offLeaves = o; o = align_up(o + leafCap * sizeof(turtle::LeafDesc), 256);
+  L.offLeavesSorted = o; o = align_up(o + leafCap * sizeof(turtle::LeafDesc), 256);
+  L.offFills = o; o = align_up(o + fillCap * sizeof(turtle::FillDesc), 256);
+  L.bytes = o;
+  return L;
+}
+
+int dtype_width(int dt) {
+  switch (dt) {
+    case TURTLE_INT8: case TURTLE_UINT8: return 1;
+    case TURTLE_INT16: case TURTLE_UINT16: return 2;
+    case TURTLE_INT32: case TURTLE_UINT32: return 4;
+    case TURTLE_INT64: case TURTLE_UINT64: return 8;
+    default: return 0;
+  }
+}
+
+unsigned long long dtype_flip(int dt) {
+  switch (dt) {
+    case TURTLE_INT8: return 0x80ull;
+    case TURTLE_INT16: return 0x8000ull;
+    case TURTLE_INT32: return 0x80000000ull;
+    case TURTLE_INT64: return 0x8000000000000000ull;
+    default: return 0ull;
+  }
+}
+
+constexpr long long kMaxElements = 1LL << 36;
+
+}  // namespace
+
+struct turtle_sorter {
+  int dtype = 0;
+  int width = 0;
+  unsigned long long flip = 0;
+  long long maxN = 0;
+  bool trackIdx = false;
+  bool compressRequested = false;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  DevBuffer keysA, idxA, keysB, idxB, ws, offsets;
+  WsLayout lay;
+  int grid[2] = {0, 0};
+  turtle::Control* hctrl = nullptr;  // pinned status block
+  // StartSorting / Sync state
+  void* hostKeys = nullptr;
+  int32_t* hostIdx = nullptr;
+  long long n = 0;
+  bool pending = false;
+  std::chrono::steady_clock::time_point t0;
+  std::atomic<long long> launches{0};
+  int lastLevels = 0;
+  std::string lastCuda;
+  struct GraphEntry {
+    void* keys; int32_t* idx; const long long* offs; long long num, total;
+    cudaGraphExec_t exec;
+  };
+  std::vector<GraphEntry> graphs;
+  std::mutex mu;
+};
+
+namespace {
+
+turtle_status from_cuda(turtle_sorter* s, cudaError_t e) {
+  if (e == cudaSuccess) return TURTLE_OK;
+  if (s) s->lastCuda = cudaGetErrorString(e);
+  cudaGetLastError();  // clear sticky-free errors
+  if (e == cudaErrorMemoryAllocation) return TURTLE_ERR_OUT_OF_MEMORY;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return TURTLE_ERR_NO_DEVICE;
+  return TURTLE_ERR_CUDA;
+}
+
+#define TRY_CUDA(s, call)                               \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return from_cuda((s), e_);   \
+  } while (0)
+
+void free_graphs(turtle_sorter* s) {
+  for (auto& g : s->graphs) cudaGraphExecDestroy(g.exec);
+  s->graphs.clear();
+}
+
+turtle_status alloc_workspace(turtle_sorter* s, long long extraLeaves) {
+  turtle::vmm_free(&s->ws);
+  s->lay = make_layout(s->maxN, turtle::kernels_tile_elems(s->width), extraLeaves);
+  TRY_CUDA(s, turtle::vmm_alloc(&s->ws, s->lay.bytes, s->device, false));
+  return TURTLE_OK;
+}
+
+turtle::SortArgs make_args(turtle_sorter* s, void* keys, int32_t* idx, const long long* offs,
+                           long long num, long long n) {
+  turtle::SortArgs a;
+  std::memset(&a, 0, sizeof(a));
+  char* w = (char*)s->ws.ptr;
+  a.keysA = keys;
+  a.idxA = idx;
+  a.keysB = s->keysB.ptr;
+  a.idxB = (int*)s->idxB.ptr;
+  a.offsets = offs;
+  a.numArrays = num;
+  a.n = n;
+  a.flip = s->flip;
+  for (int p = 0; p < 2; ++p) {
+    a.segs[p] = (turtle::SegDesc*)(w + s->lay.offSegs[p]);
+    a.tileCnt[p] = (int*)(w + s->lay.offTileCnt[p]);
+    a.tileOff[p] = (long long*)(w + s->lay.offTileOff[p]);
+  }
+  a.leaves = (turtle::LeafDesc*)(w + s->lay.offLeaves);
+  a.leavesSorted = (turtle::LeafDesc*)(w + s->lay.offLeavesSorted);
+  a.fills = (turtle::FillDesc*)(w + s->lay.offFills);
+  a.segCap = s->lay.segCap;
+  a.tileCap = s->lay.tileCap;
+  a.leafCap = s->lay.leafCap;
+  a.fillCap = s->lay.fillCap;
+  a.ctrl = (turtle::Control*)(w + s->lay.offCtrl);
+  return a;
+}
+
+// Enqueue: reset the control block, run the persistent kernel, copy the
+// control block to the pinned status block.
+cudaError_t enqueue_persistent(turtle_sorter* s, const turtle::SortArgs& a, bool hasIdx,
+                               cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(a.ctrl, 0, sizeof(turtle::Control), st);
+  if (e != cudaSuccess) return e;
+  e = turtle::kernels_launch_persistent(s->width, hasIdx, a, s->grid[hasIdx ? 1 : 0], st);
+  if (e != cudaSuccess) return e;
+  s->launches.fetch_add(1);
+  return cudaMemcpyAsync(s->hctrl, a.ctrl, sizeof(turtle::Control), cudaMemcpyDeviceToHost, st);
+}
+
+cudaStream_t pick_stream(turtle_sorter* s, void* stream) {
+  return stream ? (cudaStream_t)stream : s->stream;
+}
+
+turtle_status check_idx(turtle_sorter* s, const int32_t* idx) {
+  if (idx && !s->trackIdx) return TURTLE_ERR_INVALID_ARGUMENT;
+  return TURTLE_OK;
+}
+
+turtle_status device_status(turtle_sorter* s) {
+  s->lastLevels = s->hctrl->levels;
+  switch (s->hctrl->error) {
+    case 0: return TURTLE_OK;
+    case turtle::kDevTimeout: return TURTLE_ERR_TIMEOUT;
+    case turtle::kDevCapacity: return TURTLE_ERR_CAPACITY;
+    default: return TURTLE_ERR_CUDA;
+  }
+}
+
+turtle_status sort_device_impl(turtle_sorter* s, void* keys, int32_t* idx, long long n,
+                               cudaStream_t st) {
+  if (n < 2) return TURTLE_OK;
+  const bool hasIdx = idx != nullptr;
+  turtle::SortArgs a = make_args(s, keys, idx, nullptr, 0, n);
+  TRY_CUDA(s, enqueue_persistent(s, a, hasIdx, st));
+  return TURTLE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+turtle_status turtle_create(turtle_dtype dtype, int64_t max_n, int track_index, int compress,
+                            int device, turtle_sorter** out) {
+  if (!out) return TURTLE_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  const int width = dtype_width(dtype);
+  if (width == 0 || max_n < 0) return TURTLE_ERR_INVALID_ARGUMENT;
+  if (max_n > kMaxElements) return TURTLE_ERR_TOO_LARGE;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return TURTLE_ERR_NO_DEVICE;
+  }
+  if (device < 0) {
+    if (cudaGetDevice(&device) != cudaSuccess) return TURTLE_ERR_NO_DEVICE;
+  }
+  if (device >= ndev) return TURTLE_ERR_INVALID_ARGUMENT;
+  turtle_sorter* s = new turtle_sorter();
+  s->dtype = dtype;
+  s->width = width;
+  s->flip = dtype_flip(dtype);
+  s->maxN = max_n < 2 ? 2 : max_n;
+  s->trackIdx = track_index != 0;
+  s->compressRequested = compress != 0;
+  s->device = device;
+  auto fail = [&](turtle_status st) {
+    turtle_destroy(s);
+    return st;
+  };
+  if (cudaSetDevice(device) != cudaSuccess) return fail(TURTLE_ERR_NO_DEVICE);
+  turtle_status st;
+  cudaError_t e;
+  const size_t kbytes = (size_t)s->maxN * width;
+  const size_t ibytes = (size_t)s->maxN * sizeof(int32_t);
+  if ((e = turtle::vmm_alloc(&s->keysA, kbytes, device, s->compressRequested)) != cudaSuccess)
+    return fail(from_cuda(s, e));
+  if ((e = turtle::vmm_alloc(&s->keysB, kbytes, device, s->compressRequested)) != cudaSuccess)
+    return fail(from_cuda(s, e));
+  if (s->trackIdx) {
+    if ((e = turtle::vmm_alloc(&s->idxA, ibytes, device, s->compressRequested)) != cudaSuccess)
+      return fail(from_cuda(s, e));
+    if ((e = turtle::vmm_alloc(&s->idxB, ibytes, device, s->compressRequested)) != cudaSuccess)
+      return fail(from_cuda(s, e));
+  }
+  if ((st = alloc_workspace(s, 0)) != TURTLE_OK) return fail(st);
+  if ((e = cudaHostAlloc((void**)&s->hctrl, sizeof(turtle::Control), cudaHostAllocDefault)) !=
+      cudaSuccess)
+    return fail(from_cuda(s, e));
+  std::memset(s->hctrl, 0, sizeof(turtle::Control));
+  if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess)
+    return fail(from_cuda(s, e));
+  if ((e = turtle::kernels_prepare(width, false, device, &s->grid[0])) != cudaSuccess)
+    return fail(from_cuda(s, e));
+  if ((e = turtle::kernels_prepare(width, true, device, &s->grid[1])) != cudaSuccess)
+    return fail(from_cuda(s, e));
+  *out = s;
+  return TURTLE_OK;
+}
+
+turtle_status turtle_destroy(turtle_sorter* s) {
+  if (!s) return TURTLE_OK;
+  cudaSetDevice(s->device);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  free_graphs(s);
+  turtle::vmm_free(&s->keysA);
+  turtle::vmm_free(&s->keysB);
+  turtle::vmm_free(&s->idxA);
+  turtle::vmm_free(&s->idxB);
+  turtle::vmm_free(&s->ws);
+  turtle::vmm_free(&s->offsets);
+  if (s->hctrl) cudaFreeHost(s->hctrl);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  cudaGetLastError();
+  delete s;
+  return TURTLE_OK;
+}
+
+int turtle_compression_ok(const turtle_sorter* s) {
+  return (s && s->keysA.compressed) ? 1 : 0;
+}
+
+turtle_status turtle_start(turtle_sorter* s, void* host_keys, int32_t* host_idx, int64_t n) {
+  if (!s || (!host_keys && n > 0) || n < 0) return TURTLE_ERR_INVALID_ARGUMENT;
+  if (n > s->maxN) return TURTLE_ERR_TOO_LARGE;
+  turtle_status st = check_idx(s, host_idx);
+  if (st != TURTLE_OK) return st;
+  if (s->pending) return TURTLE_ERR_STATE;
+  cudaSetDevice(s->device);
+  s->t0 = std::chrono::steady_clock::now();
+  s->hostKeys = host_keys;
+  s->hostIdx = host_idx;
+  s->n = n;
+  std::memset(s->hctrl, 0, sizeof(turtle::Control));
+  if (n > 0) {
+    TRY_CUDA(s, cudaMemcpyAsync(s->keysA.ptr, host_keys, (size_t)n * s->width,
+                                cudaMemcpyHostToDevice, s->stream));
+    if (host_idx)
+      TRY_CUDA(s, cudaMemcpyAsync(s->idxA.ptr, host_idx, (size_t)n * sizeof(int32_t),
+                                  cudaMemcpyHostToDevice, s->stream));
+  }
+  st = sort_device_impl(s, s->keysA.ptr, host_idx ? (int32_t*)s->idxA.ptr : nullptr, n,
+                        s->stream);
+  if (st != TURTLE_OK) return st;
+  s->pending = true;
+  return TURTLE_OK;
+}
+
+turtle_status turtle_sync(turtle_sorter* s, double* seconds) {
+  if (!s) return TURTLE_ERR_INVALID_ARGUMENT;
+  if (!s->pending) return TURTLE_ERR_STATE;
+  cudaSetDevice(s->device);
+  s->pending = false;
+  TRY_CUDA(s, cudaStreamSynchronize(s->stream));
+  turtle_status st = device_status(s);
+  if (st != TURTLE_OK) return st;
+  if (s->n > 0) {
+    TRY_CUDA(s, cudaMemcpyAsync(s->hostKeys, s->keysA.ptr, (size_t)s->n * s->width,
+                                cudaMemcpyDeviceToHost, s->stream));
+    if (s->hostIdx)
+      TRY_CUDA(s, cudaMemcpyAsync(s->hostIdx, s->idxA.ptr, (size_t)s->n * sizeof(int32_t),
+                                  cudaMemcpyDeviceToHost, s->stream));
+    TRY_CUDA(s, cudaStreamSynchronize(s->stream));
+  }
+  const auto t1 = std::chrono::steady_clock::now();
+  if (seconds) *seconds = std::chrono::duration<double>(t1 - s->t0).count();
+  s->hostKeys = nullptr;
+  s->hostIdx = nullptr;
+  return TURTLE_OK;
+}
+
+turtle_status turtle_multisort_device(turtle_sorter* s, void* d_keys, int32_t* d_idx,
+                                      int64_t arr_size, int64_t num_arrays, void* stream) {
+  if (!s || arr_size < 0 || num_arrays < 0 || (!d_keys && arr_size * num_arrays > 0))
+    return TURTLE_ERR_INVALID_ARGUMENT;
+  turtle_status st = check_idx(s, d_idx);
+  if (st != TURTLE_OK) return st;
+  if (arr_size > 0 && num_arrays > s->maxN / arr_size) return TURTLE_ERR_TOO_LARGE;
+  if (arr_size < 2 || num_arrays == 0) return TURTLE_OK;
+  cudaSetDevice(s->device);
+  cudaStream_t cs = pick_stream(s, stream);
+  const int tile = turtle::kernels_tile_elems(s->width);
+  if (arr_size <= tile) {
+    TRY_CUDA(s, turtle::kernels_launch_multisort(s->width, d_idx != nullptr, d_keys, d_idx,
+                                                 num_arrays, (int)arr_size, s->flip, cs));
+    s->launches.fetch_add(1);
+    std::memset(s->hctrl, 0, sizeof(turtle::Control));
+    return TURTLE_OK;
+  }
+  // long arrays: batched persistent path with uniform offsets
+  std::vector<long long> offs((size_t)num_arrays + 1);
+  for (long long i = 0; i <= num_arrays; ++i) offs[(size_t)i] = i * arr_size;
+  const size_t ob = offs.size() * sizeof(long long);
+  if (s->offsets.bytes < ob) {
+    TRY_CUDA(s, cudaStreamSynchronize(cs));
+    turtle::vmm_free(&s->offsets);
+    TRY_CUDA(s, turtle::vmm_alloc(&s->offsets, ob, s->device, false));
+  }
+  TRY_CUDA(s, cudaMemcpyAsync(s->offsets.ptr, offs.data(), ob, cudaMemcpyHostToDevice, cs));
+  TRY_CUDA(s, cudaStreamSynchronize(cs));  // offs is a host temporary
+  return turtle_sort_batched_device(s, d_keys, d_idx, (const int64_t*)s->offsets.ptr, num_arrays,
+                                    arr_size * num_arrays, stream);
+}
+
+turtle_status turtle_multisort(turtle_sorter* s, void* host_keys, int64_t arr_size,
+                               int64_t num_arrays, int block_size, double* seconds) {
+  if (!s || arr_size < 0 || num_arrays < 0 || (!host_keys && arr_size * num_arrays > 0))
+    return TURTLE_ERR_INVALID_ARGUMENT;
+  if (block_size > 0 && num_arrays % block_size != 0) return TURTLE_ERR_INVALID_ARGUMENT;
+  if (arr_size > 0 && num_arrays > s->maxN / arr_size) return TURTLE_ERR_TOO_LARGE;
+  if (s->pending) return TURTLE_ERR_STATE;
+  cudaSetDevice(s->device);
+  const auto t0 = std::chrono::steady_clock::now();
+  const size_t bytes = (size_t)(arr_size * num_arrays) * s->width;
+  if (bytes > 0) {
+    TRY_CUDA(s, cudaMemcpyAsync(s->keysA.ptr, host_keys, bytes, cudaMemcpyHostToDevice, s->stream));
+    turtle_status st =
+        turtle_multisort_device(s, s->keysA.ptr, nullptr, arr_size, num_arrays, s->stream);
+    if (st != TURTLE_OK) return st;
+    TRY_CUDA(s, cudaMemcpyAsync(host_keys, s->keysA.ptr, bytes, cudaMemcpyDeviceToHost, s->stream));
+    TRY_CUDA(s, cudaStreamSynchronize(s->stream));
+    st = device_status(s);
+    if (st != TURTLE_OK) return st;
+  }
+  const auto t1 = std::chrono::steady_clock::now();
+  if (seconds) *seconds = std::chrono::duration<double>(t1 - t0).count();
+  return TURTLE_OK;
+}
+
+turtle_status turtle_sort_device(turtle_sorter* s, void* d_keys, int32_t* d_idx, int64_t n,
+                                 void* stream) {
+  if (!s || n < 0 || (!d_keys && n > 0)) return TURTLE_ERR_INVALID_ARGUMENT;
+  if (n > s->maxN) return TURTLE_ERR_TOO_LARGE;
+  turtle_status st = check_idx(s, d_idx);
+  if (st != TURTLE_OK) return st;
+  if (((uintptr_t)d_keys % s->width) != 0 || ((uintptr_t)d_idx % 4) != 0)
+    return TURTLE_ERR_ALIGNMENT;
+  cudaSetDevice(s->device);
+  std::memset(s->hctrl, 0, sizeof(turtle::Control));
+  return sort_device_impl(s, d_keys, d_idx, n, pick_stream(s, stream));
+}
+
+turtle_status turtle_sort_batched_device(turtle_sorter* s, void* d_keys, int32_t* d_idx,
+                                         const int64_t* d_offsets, int64_t num, int64_t total,
+                                         void* stream) {
+  if (!s || num < 0 || total < 0 || (num > 0 && (!d_offsets || (!d_keys && total > 0))))
+    return TURTLE_ERR_INVALID_ARGUMENT;
+  if (total > s->maxN) return TURTLE_ERR_TOO_LARGE;
+  turtle_status st = check_idx(s, d_idx);
+  if (st != TURTLE_OK) return st;
+  if (((uintptr_t)d_keys % s->width) != 0 || ((uintptr_t)d_idx % 4) != 0 ||
+      ((uintptr_t)d_offsets % 8) != 0)
+    return TURTLE_ERR_ALIGNMENT;
+  cudaSetDevice(s->device);
+  std::memset(s->hctrl, 0, sizeof(turtle::Control));
+  if (num == 0 || total < 2) return TURTLE_OK;
+  cudaStream_t cs = pick_stream(s, stream);
+  std::lock_guard<std::mutex> lk(s->mu);
+  // every small array may become one leaf at once
+  if ((long long)s->lay.leafCap < num + 8LL * (s->lay.segCap + 1) + 1024) {
+    TRY_CUDA(s, cudaDeviceSynchronize());
+    free_graphs(s);
+    if ((st = alloc_workspace(s, num)) != TURTLE_OK) return st;
+  }
+  const bool hasIdx = d_idx != nullptr;
+  for (auto& g : s->graphs) {
+    if (g.keys == d_keys && g.idx == d_idx && g.offs == (const long long*)d_offsets &&
+        g.num == num && g.total == total) {
+      TRY_CUDA(s, cudaGraphLaunch(g.exec, cs));
+      s->launches.fetch_add(1);
+      return TURTLE_OK;
+    }
+  }
+  turtle::SortArgs a = make_args(s, d_keys, d_idx, (const long long*)d_offsets, num, total);
+  // capture memset + persistent kernel + status copy into a graph
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  TRY_CUDA(s, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t ce = enqueue_persistent(s, a, hasIdx, s->stream);
+  s->launches.fetch_sub(1);  // counted when the graph is launched
+  cudaError_t ee = cudaStreamEndCapture(s->stream, &graph);
+  if (ce != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return from_cuda(s, ce); }
+  if (ee != cudaSuccess) return from_cuda(s, ee);
+  ee = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ee != cudaSuccess) return from_cuda(s, ee);
+  if (s->graphs.size() >= 16) {
+    cudaGraphExecDestroy(s->graphs.front().exec);
+    s->graphs.erase(s->graphs.begin());
+  }
+  s->graphs.push_back({d_keys, d_idx, (const long long*)d_offsets, num, total, exec});
+  TRY_CUDA(s, cudaGraphLaunch(exec, cs));
+  s->launches.fetch_add(1);
+  return TURTLE_OK;
+}
+
+turtle_status turtle_stream_status(turtle_sorter* s, void* stream) {
+  if (!s) return TURTLE_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(s->device);
+  TRY_CUDA(s, cudaStreamSynchronize(pick_stream(s, stream)));
+  return device_status(s);
+}
+
+int64_t turtle_launch_count(const turtle_sorter* s) { return s ? s->launches.load() : 0; }
+
+int turtle_last_levels(const turtle_sorter* s) { return s ? s->lastLevels : 0; }
+
+int64_t turtle_max_elements(turtle_dtype dtype, int track_index) {
+  (void)track_index;
+  return dtype_width(dtype) ? kMaxElements : 0;
+}
+
+int64_t turtle_smem_capacity(turtle_dtype dtype, int track_index) {
+  (void)track_index;
+  const int w = dtype_width(dtype);
+  return w ? turtle::kernels_tile_elems(w) : 0;
+}
+
+const char* turtle_status_string(turtle_status st) {
+  switch (st) {
+    case TURTLE_OK: return "ok";
+    case TURTLE_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case TURTLE_ERR_TOO_LARGE: return "size above the sorter's capacity";
+    case TURTLE_ERR_CUDA: return "CUDA error";
+    case TURTLE_ERR_OUT_OF_MEMORY: return "out of memory";
+    case TURTLE_ERR_TIMEOUT: return "device-side wait timed out";
+    case TURTLE_ERR_CAPACITY: return "device work list capacity exceeded";
+    case TURTLE_ERR_STATE: return "call out of order";
+    case TURTLE_ERR_ALIGNMENT: return "misaligned device pointer";
+    case TURTLE_ERR_NO_DEVICE: return "no CUDA device";
+    case TURTLE_ERR_BUDGET: return "request larger than the memory budget";
+    default: return "unknown status";
+  }
+}
+
+const char* turtle_last_cuda_error(const turtle_sorter* s) {
+  return s ? s->lastCuda.c_str() : "";
+}
+
+void turtle_debug_fail_allocations(int count) { turtle::vmm_inject_failures(count); }
+
+const char* turtle_version(void) { return "turtle-gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

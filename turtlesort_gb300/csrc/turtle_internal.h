@@ -1,0 +1,45 @@
+// Internal declarations shared by the kernel and host translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+
+namespace turtle {
+
+struct SortArgs;
+
+// ---- kernels (turtle_sort.cu) ----
+// width = key bytes (1, 2, 4, 8); hasIdx = int32 payload present.
+cudaError_t kernels_prepare(int width, bool hasIdx, int device, int* grid);
+cudaError_t kernels_launch_persistent(int width, bool hasIdx, const SortArgs& a, int grid,
+                                      cudaStream_t stream);
+cudaError_t kernels_launch_multisort(int width, bool hasIdx, void* keys, int* idx,
+                                     long long numArrays, int arrSize, unsigned long long flip,
+                                     cudaStream_t stream);
+int kernels_tile_elems(int width);
+
+// ---- device buffers on the driver VMM API (turtle_vmm.cu) ----
+// Replaces TurtleBuffer::Buffer (turtle-buffer.cuh:7-100) and
+// QuickHelper::allocateCompressible/freeCompressible (quick-helper.cuh:39-127).
+struct DevBuffer {
+  void* ptr = nullptr;
+  size_t bytes = 0;        // requested
+  size_t mapped = 0;       // rounded to the allocation granularity
+  bool vmm = false;        // false: cudaMalloc fallback
+  bool compressed = false; // generic compression really granted
+};
+
+// Allocates `bytes` on `device`.  want_compression asks for
+// CU_MEM_ALLOCATION_COMP_GENERIC; if the device does not support it or the
+// driver does not grant it, the buffer is allocated uncompressed.  Returns a
+// CUDA error code (cudaSuccess on success).
+cudaError_t vmm_alloc(DevBuffer* b, size_t bytes, int device, bool want_compression);
+void vmm_free(DevBuffer* b);
+bool vmm_compression_supported(int device);
+
+// Test hook: make the next `count` VMM allocations fail (host-side fault
+// injection; the buffer layer then reports cudaErrorMemoryAllocation).
+void vmm_inject_failures(int count);
+
+}  // namespace turtle
