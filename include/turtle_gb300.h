@@ -151,6 +151,13 @@ const char* turtle_last_cuda_error(const turtle_sorter* s);
  * involved; callers see TURTLE_ERR_OUT_OF_MEMORY. */
 void turtle_debug_fail_allocations(int count);
 
+/* Phase timeline of the last persistent-kernel sort (valid after
+ * turtle_stream_status / turtle_sync): globaltimer nanoseconds taken after
+ * each grid barrier, with the work items of the phase that ended there, and a
+ * final entry (info = -2) when the last CTA finished.  Returns the number of
+ * entries written (at most max). */
+int turtle_debug_timeline(const turtle_sorter* s, uint64_t* ns, int32_t* info, int max);
+
 /* Library version string (static storage). */
 const char* turtle_version(void);
 

@@ -36,7 +36,7 @@ def test_python_binding_covers_header(native_lib):
 def test_host_side_answers(native_lib):
     assert native_lib.turtle_status_string(0) == b"ok"
     assert b"capacity" in native_lib.turtle_status_string(6)
-    assert native_lib.turtle_max_elements(4, 1) >= 1 << 31
+    assert native_lib.turtle_max_elements(4, 1) == (1 << 31) - 1
     assert native_lib.turtle_max_elements(99, 1) == 0
     assert native_lib.turtle_smem_capacity(4, 1) == 8192
     assert native_lib.turtle_smem_capacity(6, 1) == 4096
@@ -53,6 +53,7 @@ def test_create_bad_arguments(native_lib):
     assert native_lib.turtle_create(42, 10, 1, 0, -1, C.byref(h)) == 1  # bad dtype
     assert native_lib.turtle_create(4, -1, 1, 0, -1, C.byref(h)) == 1   # negative size
     assert native_lib.turtle_create(4, 1 << 40, 1, 0, -1, C.byref(h)) == 2  # too large
+    assert native_lib.turtle_create(4, 1 << 31, 1, 0, -1, C.byref(h)) == 2
 
 
 @pytest.mark.skipif(has_gpu(), reason="checks the no-device path")

@@ -47,7 +47,8 @@ def make_keys(dtype, n, dist, seed):
         pick = (dg.splitmix64(seed, 0, n) % np.uint64(pool.size)).astype(np.int64)
         return pool[pick]
     if dist == "two":
-        return np.where(dg.uniform(np.uint8, n, seed) & 1, hi, lo).astype(dtype)
+        pair = np.array([lo, hi], dtype=dtype)
+        return pair[(dg.uniform(np.uint8, n, seed) & 1).astype(np.int64)]
     raise ValueError(dist)
 
 

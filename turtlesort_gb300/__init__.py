@@ -52,6 +52,17 @@ def smem_capacity(dtype, track_index: bool = True) -> int:
     return int(load_library().turtle_smem_capacity(dtype_code(dtype), int(track_index)))
 
 
+CUDA_STREAM_LEGACY = 1  # cudaStreamLegacy: the legacy default stream
+
+
+def _stream(stream) -> Optional[C.c_void_p]:
+    """None -> the sorter's own stream (NULL in the C ABI); 0 -> the legacy
+    default stream (torch's default stream handle is 0); else the handle."""
+    if stream is None:
+        return None
+    return C.c_void_p(CUDA_STREAM_LEGACY if int(stream) == 0 else int(stream))
+
+
 def _check(st: int, where: str, handle=None) -> None:
     if st != 0:
         detail = ""
@@ -147,34 +158,45 @@ class TurtleSort:
         return float(secs.value)
 
     # -- device-resident forms --
-    def sort_device(self, keys_ptr: int, idx_ptr: Optional[int], n: int, stream: int = 0) -> None:
+    def sort_device(self, keys_ptr: int, idx_ptr: Optional[int], n: int, stream=None) -> None:
+        """Sorts on ``stream`` (a CUDA stream handle; 0 = legacy default stream,
+        None = the sorter's own stream).  Asynchronous."""
         st = self._lib.turtle_sort_device(self._h, C.c_void_p(keys_ptr),
                                           C.c_void_p(idx_ptr) if idx_ptr else None, int(n),
-                                          C.c_void_p(stream) if stream else None)
+                                          _stream(stream))
         _check(st, "sort_device", self._h)
 
     def sort_batched_device(self, keys_ptr: int, idx_ptr: Optional[int], offsets_ptr: int,
-                            num: int, total: int, stream: int = 0) -> None:
+                            num: int, total: int, stream=None) -> None:
         st = self._lib.turtle_sort_batched_device(
             self._h, C.c_void_p(keys_ptr), C.c_void_p(idx_ptr) if idx_ptr else None,
-            C.c_void_p(offsets_ptr), int(num), int(total), C.c_void_p(stream) if stream else None)
+            C.c_void_p(offsets_ptr), int(num), int(total), _stream(stream))
         _check(st, "sort_batched_device", self._h)
 
     def multisort_device(self, keys_ptr: int, idx_ptr: Optional[int], arr_size: int,
-                         num_arrays: int, stream: int = 0) -> None:
+                         num_arrays: int, stream=None) -> None:
         st = self._lib.turtle_multisort_device(
             self._h, C.c_void_p(keys_ptr), C.c_void_p(idx_ptr) if idx_ptr else None,
-            int(arr_size), int(num_arrays), C.c_void_p(stream) if stream else None)
+            int(arr_size), int(num_arrays), _stream(stream))
         _check(st, "multisort_device", self._h)
 
-    def status(self, stream: int = 0) -> None:
-        """Waits for ``stream`` and raises if the device reported an error."""
-        st = self._lib.turtle_stream_status(self._h, C.c_void_p(stream) if stream else None)
+    def status(self, stream=None) -> None:
+        """Waits for ``stream`` (None = the sorter's own stream) and raises if
+        the device reported an error."""
+        st = self._lib.turtle_stream_status(self._h, _stream(stream))
         _check(st, "device status", self._h)
 
     @property
     def launches(self) -> int:
         return int(self._lib.turtle_launch_count(self._h))
+
+    def timeline(self):
+        """(ns, info) arrays of the last persistent sort's phase timeline."""
+        ns = np.zeros(256, dtype=np.uint64)
+        info = np.zeros(256, dtype=np.int32)
+        n = self._lib.turtle_debug_timeline(self._h, ns.ctypes.data_as(C.c_void_p),
+                                            info.ctypes.data_as(C.c_void_p), 256)
+        return ns[:n], info[:n]
 
     @property
     def last_levels(self) -> int:

@@ -51,6 +51,7 @@ SIGNATURES = [
     ("turtle_last_cuda_error", C.c_char_p, [_P]),
     ("turtle_debug_fail_allocations", None, [_I]),
     ("turtle_version", C.c_char_p, []),
+    ("turtle_debug_timeline", _I, [_P, _P, _P, _I]),
 ]
 
 _lib = None

@@ -26,18 +26,23 @@ namespace {
 
 struct WsLayout {
   int segCap = 0, tileCap = 0, leafCap = 0, fillCap = 0;
-  size_t offCtrl = 0, offSegs[2] = {0, 0}, offTileCnt[2] = {0, 0}, offTileOff[2] = {0, 0};
+  size_t offWarpCnt[2] = {0, 0};
+  size_t offCtrl = 0, offSegs[2] = {0, 0}, offTiles[2] = {0, 0}, offTileCnt[2] = {0, 0},
+         offTileOff[2] = {0, 0};
   size_t offLeaves = 0, offLeavesSorted = 0, offFills = 0, bytes = 0;
 };
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
-WsLayout make_layout(long long maxN, int tile, long long extraLeaves) {
+WsLayout make_layout(long long maxN, int tile, int leafMax, long long extraLeaves) {
   WsLayout L;
-  const long long segCap = maxN / tile + 66;
+  // segments of one level are disjoint and longer than leafMax
+  const long long segCap = maxN / leafMax + 66;
   const long long tileCap = maxN / tile + 2 * segCap + 64;
-  const long long leafCap = 8 * (segCap + 1) + extraLeaves + 1024;
-  const long long fillCap = 2 * (3 * (segCap + 1) + tileCap) + 1024;
+  // leaf / fill lists: roomy enough that a partition never has to yield on
+  // ordinary inputs (one level adds at most 4 leaves and 3 fills per segment)
+  const long long leafCap = std::max(8 * (segCap + 1), maxN / 64) + extraLeaves + 4096;
+  const long long fillCap = 2 * (3 * (segCap + 1) + tileCap) + maxN / 64 + 4096;
   L.segCap = (int)segCap;
   L.tileCap = (int)tileCap;
   L.leafCap = (int)leafCap;
@@ -45,8 +50,11 @@ WsLayout make_layout(long long maxN, int tile, long long extraLeaves) {
   size_t o = 0;
   L.offCtrl = o; o = align_up(o + sizeof(turtle::Control), 256);
   for (int p = 0; p < 2; ++p) { L.offSegs[p] = o; o = align_up(o + segCap * sizeof(turtle::SegDesc), 256); }
+  for (int p = 0; p < 2; ++p) { L.offTiles[p] = o; o = align_up(o + tileCap * sizeof(turtle::TileDesc), 256); }
   for (int p = 0; p < 2; ++p) { L.offTileCnt[p] = o; o = align_up(o + tileCap * 8 * sizeof(int), 256); }
   for (int p = 0; p < 2; ++p) { L.offTileOff[p] = o; o = align_up(o + tileCap * 8 * sizeof(long long), 256); }
+  // per-warp-chunk counts: kThreads / 32 chunks per tile (the partition CTA's warps)
+  for (int p = 0; p < 2; ++p) { L.offWarpCnt[p] = o; o = align_up(o + tileCap * 16 * 8 * sizeof(int), 256); }
   L.offLeaves = o; o = align_up(o + leafCap * sizeof(turtle::LeafDesc), 256);
   L.offLeavesSorted = o; o = align_up(o + leafCap * sizeof(turtle::LeafDesc), 256);
   L.offFills = o; o = align_up(o + fillCap * sizeof(turtle::FillDesc), 256);
@@ -74,7 +82,7 @@ unsigned long long dtype_flip(int dt) {
   }
 }
 
-constexpr long long kMaxElements = 1LL << 36;
+constexpr long long kMaxElements = (1LL << 31) - 1;  // int32 ids and in-segment offsets
 
 }  // namespace
 
@@ -106,6 +114,11 @@ struct turtle_sorter {
   };
   std::vector<GraphEntry> graphs;
   std::mutex mu;
+  // last persistent launch, for resuming a partition that yielded
+  turtle::SortArgs lastArgs;
+  bool lastHasIdx = false;
+  bool lastValid = false;
+  cudaStream_t lastStream = nullptr;
 };
 
 namespace {
@@ -132,7 +145,8 @@ void free_graphs(turtle_sorter* s) {
 
 turtle_status alloc_workspace(turtle_sorter* s, long long extraLeaves) {
   turtle::vmm_free(&s->ws);
-  s->lay = make_layout(s->maxN, turtle::kernels_tile_elems(s->width), extraLeaves);
+  s->lay = make_layout(s->maxN, turtle::kernels_tile_elems(s->width),
+                       turtle::kernels_leaf_max(s->width), extraLeaves);
   TRY_CUDA(s, turtle::vmm_alloc(&s->ws, s->lay.bytes, s->device, false));
   return TURTLE_OK;
 }
@@ -152,7 +166,9 @@ turtle::SortArgs make_args(turtle_sorter* s, void* keys, int32_t* idx, const lon
   a.flip = s->flip;
   for (int p = 0; p < 2; ++p) {
     a.segs[p] = (turtle::SegDesc*)(w + s->lay.offSegs[p]);
+    a.tiles[p] = (turtle::TileDesc*)(w + s->lay.offTiles[p]);
     a.tileCnt[p] = (int*)(w + s->lay.offTileCnt[p]);
+    a.warpCnt[p] = (int*)(w + s->lay.offWarpCnt[p]);
     a.tileOff[p] = (long long*)(w + s->lay.offTileOff[p]);
   }
   a.leaves = (turtle::LeafDesc*)(w + s->lay.offLeaves);
@@ -170,13 +186,25 @@ turtle::SortArgs make_args(turtle_sorter* s, void* keys, int32_t* idx, const lon
 // control block to the pinned status block.
 cudaError_t enqueue_persistent(turtle_sorter* s, const turtle::SortArgs& a, bool hasIdx,
                                cudaStream_t st) {
-  cudaError_t e = cudaMemsetAsync(a.ctrl, 0, sizeof(turtle::Control), st);
+  if (!a.resume) {
+    cudaError_t e = cudaMemsetAsync(a.ctrl, 0, sizeof(turtle::Control), st);
+    if (e != cudaSuccess) return e;
+  }
+  cudaError_t e = turtle::kernels_launch_persistent(s->width, hasIdx, a, s->grid[hasIdx ? 1 : 0], st);
   if (e != cudaSuccess) return e;
-  e = turtle::kernels_launch_persistent(s->width, hasIdx, a, s->grid[hasIdx ? 1 : 0], st);
-  if (e != cudaSuccess) return e;
-  s->launches.fetch_add(1);
+  s->launches.fetch_add(2);  // partition + leaf kernel
+  s->lastArgs = a;
+  s->lastArgs.resume = 1;
+  s->lastHasIdx = hasIdx;
+  s->lastStream = st;
+  s->lastValid = true;
   return cudaMemcpyAsync(s->hctrl, a.ctrl, sizeof(turtle::Control), cudaMemcpyDeviceToHost, st);
 }
+
+// After the stream of the last sort has been synchronized: if the partition
+// yielded (its leaf lists filled up), relaunch it from the saved level until
+// it completes.  Only pathological inputs ever take this path.
+turtle_status finish_yields(turtle_sorter* s);
 
 cudaStream_t pick_stream(turtle_sorter* s, void* stream) {
   return stream ? (cudaStream_t)stream : s->stream;
@@ -188,6 +216,8 @@ turtle_status check_idx(turtle_sorter* s, const int32_t* idx) {
 }
 
 turtle_status device_status(turtle_sorter* s) {
+  turtle_status y = finish_yields(s);
+  if (y != TURTLE_OK) return y;
   s->lastLevels = s->hctrl->levels;
   switch (s->hctrl->error) {
     case 0: return TURTLE_OK;
@@ -195,6 +225,16 @@ turtle_status device_status(turtle_sorter* s) {
     case turtle::kDevCapacity: return TURTLE_ERR_CAPACITY;
     default: return TURTLE_ERR_CUDA;
   }
+}
+
+turtle_status finish_yields(turtle_sorter* s) {
+  int rounds = 0;
+  while (s->lastValid && s->hctrl->error == 0 && s->hctrl->yield != 0) {
+    if (++rounds > 100000) return TURTLE_ERR_CAPACITY;
+    TRY_CUDA(s, enqueue_persistent(s, s->lastArgs, s->lastHasIdx, s->lastStream));
+    TRY_CUDA(s, cudaStreamSynchronize(s->lastStream));
+  }
+  return TURTLE_OK;
 }
 
 turtle_status sort_device_impl(turtle_sorter* s, void* keys, int32_t* idx, long long n,
@@ -349,8 +389,8 @@ turtle_status turtle_multisort_device(turtle_sorter* s, void* d_keys, int32_t* d
   if (arr_size < 2 || num_arrays == 0) return TURTLE_OK;
   cudaSetDevice(s->device);
   cudaStream_t cs = pick_stream(s, stream);
-  const int tile = turtle::kernels_tile_elems(s->width);
-  if (arr_size <= tile) {
+  const int leafMax = turtle::kernels_leaf_max(s->width);
+  if (arr_size <= leafMax) {
     TRY_CUDA(s, turtle::kernels_launch_multisort(s->width, d_idx != nullptr, d_keys, d_idx,
                                                  num_arrays, (int)arr_size, s->flip, cs));
     s->launches.fetch_add(1);
@@ -403,7 +443,7 @@ turtle_status turtle_sort_device(turtle_sorter* s, void* d_keys, int32_t* d_idx,
   if (n > s->maxN) return TURTLE_ERR_TOO_LARGE;
   turtle_status st = check_idx(s, d_idx);
   if (st != TURTLE_OK) return st;
-  if (((uintptr_t)d_keys % s->width) != 0 || ((uintptr_t)d_idx % 4) != 0)
+  if (((uintptr_t)d_keys % 16) != 0 || ((uintptr_t)d_idx % 16) != 0)
     return TURTLE_ERR_ALIGNMENT;
   cudaSetDevice(s->device);
   std::memset(s->hctrl, 0, sizeof(turtle::Control));
@@ -418,7 +458,7 @@ turtle_status turtle_sort_batched_device(turtle_sorter* s, void* d_keys, int32_t
   if (total > s->maxN) return TURTLE_ERR_TOO_LARGE;
   turtle_status st = check_idx(s, d_idx);
   if (st != TURTLE_OK) return st;
-  if (((uintptr_t)d_keys % s->width) != 0 || ((uintptr_t)d_idx % 4) != 0 ||
+  if (((uintptr_t)d_keys % 16) != 0 || ((uintptr_t)d_idx % 16) != 0 ||
       ((uintptr_t)d_offsets % 8) != 0)
     return TURTLE_ERR_ALIGNMENT;
   cudaSetDevice(s->device);
@@ -427,7 +467,7 @@ turtle_status turtle_sort_batched_device(turtle_sorter* s, void* d_keys, int32_t
   cudaStream_t cs = pick_stream(s, stream);
   std::lock_guard<std::mutex> lk(s->mu);
   // every small array may become one leaf at once
-  if ((long long)s->lay.leafCap < num + 8LL * (s->lay.segCap + 1) + 1024) {
+  if ((long long)s->lay.leafCap < num + 8LL * (s->lay.segCap + 1) + 4096) {
     TRY_CUDA(s, cudaDeviceSynchronize());
     free_graphs(s);
     if ((st = alloc_workspace(s, num)) != TURTLE_OK) return st;
@@ -437,7 +477,12 @@ turtle_status turtle_sort_batched_device(turtle_sorter* s, void* d_keys, int32_t
     if (g.keys == d_keys && g.idx == d_idx && g.offs == (const long long*)d_offsets &&
         g.num == num && g.total == total) {
       TRY_CUDA(s, cudaGraphLaunch(g.exec, cs));
-      s->launches.fetch_add(1);
+      s->launches.fetch_add(2);
+      s->lastArgs = make_args(s, d_keys, d_idx, (const long long*)d_offsets, num, total);
+      s->lastArgs.resume = 1;
+      s->lastHasIdx = hasIdx;
+      s->lastStream = cs;
+      s->lastValid = true;
       return TURTLE_OK;
     }
   }
@@ -447,7 +492,7 @@ turtle_status turtle_sort_batched_device(turtle_sorter* s, void* d_keys, int32_t
   cudaGraphExec_t exec = nullptr;
   TRY_CUDA(s, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
   cudaError_t ce = enqueue_persistent(s, a, hasIdx, s->stream);
-  s->launches.fetch_sub(1);  // counted when the graph is launched
+  s->launches.fetch_sub(2);  // counted when the graph is launched
   cudaError_t ee = cudaStreamEndCapture(s->stream, &graph);
   if (ce != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return from_cuda(s, ce); }
   if (ee != cudaSuccess) return from_cuda(s, ee);
@@ -460,7 +505,8 @@ turtle_status turtle_sort_batched_device(turtle_sorter* s, void* d_keys, int32_t
   }
   s->graphs.push_back({d_keys, d_idx, (const long long*)d_offsets, num, total, exec});
   TRY_CUDA(s, cudaGraphLaunch(exec, cs));
-  s->launches.fetch_add(1);
+  s->launches.fetch_add(2);
+  s->lastStream = cs;
   return TURTLE_OK;
 }
 
@@ -483,7 +529,7 @@ int64_t turtle_max_elements(turtle_dtype dtype, int track_index) {
 int64_t turtle_smem_capacity(turtle_dtype dtype, int track_index) {
   (void)track_index;
   const int w = dtype_width(dtype);
-  return w ? turtle::kernels_tile_elems(w) : 0;
+  return w ? turtle::kernels_leaf_max(w) : 0;
 }
 
 const char* turtle_status_string(turtle_status st) {
@@ -508,6 +554,19 @@ const char* turtle_last_cuda_error(const turtle_sorter* s) {
 }
 
 void turtle_debug_fail_allocations(int count) { turtle::vmm_inject_failures(count); }
+
+int turtle_debug_timeline(const turtle_sorter* s, uint64_t* ns, int32_t* info, int max) {
+  if (!s || !s->hctrl) return 0;
+  const int n = std::min(std::min(s->hctrl->tlCount, turtle::kTimeline), max - 1);
+  if (n <= 0) return 0;
+  for (int i = 0; i < n; ++i) {
+    ns[i] = s->hctrl->tl[i];
+    info[i] = s->hctrl->tlInfo[i];
+  }
+  ns[n] = s->hctrl->tEnd;
+  info[n] = -2;
+  return n + 1;
+}
 
 const char* turtle_version(void) { return "turtle-gb300 0.1 (sm_103a)"; }
 

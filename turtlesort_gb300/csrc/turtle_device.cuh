@@ -15,18 +15,22 @@
 
 #include <cuda/atomic>
 #include <cstdint>
+#include <type_traits>
 
 namespace turtle {
 
-constexpr int kThreads = 512;            // CTA size of every sort kernel
+constexpr int kThreads = 512;            // CTA size of the partition kernel
 constexpr int kWarps = kThreads / 32;
-constexpr int kMinBlocks = 2;            // resident CTAs per SM we compile for
+constexpr int kMinBlocks = 2;            // resident partition CTAs per SM we compile for
+constexpr int kLThreads = 512;           // CTA size of the leaf / batched kernels
+constexpr int kLWarps = kLThreads / 32;
 constexpr int kFillChunk = 1 << 16;      // pivot-run fill work unit (elements)
 constexpr int kDepthSwitch = 48;         // levels of start/mid/stop pivots before
                                          // switching to sampled quartile pivots
 constexpr int kMaxLevels = 4096;         // hard cap on partition levels
 constexpr int kLeafClasses = 10;         // group sizes 1, 2, 4, ..., 512 threads
 constexpr long long kSpinLimit = 40000000LL;  // bounded barrier spin iterations
+constexpr int kTimeline = 160;           // phase timestamps kept per launch
 
 // Device status words (match turtle_status in turtle_gb300.h)
 constexpr int kDevOk = 0;
@@ -36,20 +40,27 @@ constexpr int kDevCapacity = 6;
 // Key width traits: KT is the in-kernel key word, kItems the elements per
 // thread for both the partition tile and the shared-memory sort.
 template <typename U> struct KeyCfg;
-template <> struct KeyCfg<uint8_t> { using KT = uint32_t; static constexpr int kItems = 16; };
-template <> struct KeyCfg<uint16_t> { using KT = uint32_t; static constexpr int kItems = 16; };
-template <> struct KeyCfg<uint32_t> { using KT = uint32_t; static constexpr int kItems = 16; };
-template <> struct KeyCfg<uint64_t> { using KT = uint64_t; static constexpr int kItems = 8; };
+// kItems: per thread in the partition kernel; kLItems: per thread in the
+// shared-memory (leaf / batched) sort.
+template <> struct KeyCfg<uint8_t> { using KT = uint32_t; static constexpr int kItems = 8, kLItems = 16; };
+template <> struct KeyCfg<uint16_t> { using KT = uint32_t; static constexpr int kItems = 8, kLItems = 16; };
+template <> struct KeyCfg<uint32_t> { using KT = uint32_t; static constexpr int kItems = 8, kLItems = 16; };
+template <> struct KeyCfg<uint64_t> { using KT = uint64_t; static constexpr int kItems = 8, kLItems = 8; };
 
 template <typename U>
 struct Geom {
   using KT = typename KeyCfg<U>::KT;
   static constexpr int kItems = KeyCfg<U>::kItems;
-  static constexpr int kTile = kThreads * kItems;       // partition tile = smem sort capacity
-  static constexpr int kWarpChunk = 32 * kItems;        // elements per warp in a tile
+  static constexpr int kLItems = KeyCfg<U>::kLItems;
+  static constexpr int kTile = kThreads * kItems;       // partition tile
+  static constexpr int kLeafMax = kLThreads * kLItems;  // shared-memory sort capacity
+  static constexpr int kWarpChunk = 32 * kItems;        // elements per warp chunk
+  static constexpr int kChunks = kTile / kWarpChunk;    // warp chunks per tile
   static constexpr int kKeyPadShift = sizeof(KT) == 8 ? 4 : 5;
   static constexpr int kKeySlots = kTile + (kTile >> kKeyPadShift) + 8;
   static constexpr int kIdxSlots = kTile + (kTile >> 5) + 8;
+  static constexpr int kLeafKeySlots = kLeafMax + (kLeafMax >> kKeyPadShift) + 8;
+  static constexpr int kLeafIdxSlots = kLeafMax + (kLeafMax >> 5) + 8;
 };
 
 // Bank-conflict padding for shared-memory element arrays.
@@ -71,6 +82,19 @@ struct SegDesc {        // a segment partitioned by the multi-CTA 3-pivot pass
   int tileBase;         // first entry in this level's tile arrays
   int ntiles;
   int done;             // count-phase tiles finished (last one plans)
+  int pad;
+  unsigned long long piv[3];  // pivot candidates a[start+n/2], a[start], a[stop]
+                              // (unsigned images; captured by the parent's scatter)
+  long long cbase[8];   // class boundaries after planning (cbase[7] = end)
+  int childSeg[4];      // next-level segment of classes 0,2,4,6 (-1: none)
+  unsigned long long pivS[3];  // sorted pivots (unsigned images), set by the plan
+  unsigned lut;         // class remap for equal pivots, set by the plan
+  int pad2;
+};
+struct TileDesc {       // one partition tile: [lo, hi) of segment seg
+  long long lo;
+  long long hi;
+  int seg;
   int pad;
 };
 struct LeafDesc {       // a segment finished by the shared-memory sort
@@ -96,7 +120,20 @@ struct Control {
   unsigned int barGen;
   int error;
   int levels;
-  int pad[2];
+  int tlCount;                    // timeline entries written (block 0)
+  int finished;                   // CTAs that reached the end of the kernel
+  int leafItems;                  // leaf work items left for the leaf kernel
+  int fillItems;                  // parked pivot-run fills left for the leaf kernel
+  int classItemsG[16];            // first leaf item of each size class
+  int classOffG[16];              // first sorted leaf of each size class
+  unsigned int leafWork;          // leaf-kernel work counter
+  int leafDone;                   // leaf-kernel CTAs finished
+  int yield;                      // 1: partition stopped early to drain the leaf lists
+  int resumeLevel;                // level to continue from after a yield
+  int resumePhase;                // work-counter ring position at the yield
+  unsigned long long tEnd;        // globaltimer when the last CTA finished
+  unsigned long long tl[kTimeline];  // globaltimer (ns) after each grid barrier
+  int tlInfo[kTimeline];             // work items of the phase that just ended
 };
 
 struct SortArgs {
@@ -109,12 +146,15 @@ struct SortArgs {
   long long n;
   unsigned long long flip;   // sign-bit mask for signed dtypes (0 otherwise)
   SegDesc* segs[2];
-  int* tileCnt[2];           // [tile][8] class counts
+  TileDesc* tiles[2];
+  int* tileCnt[2];           // [tile][8] class counts (summed over the tile's warps)
+  int* warpCnt[2];           // [tile][kChunks][8] class counts per warp chunk
   long long* tileOff[2];     // [tile][8] global destination of each class
   LeafDesc* leaves;
   LeafDesc* leavesSorted;
   FillDesc* fills;
   int segCap, tileCap, leafCap, fillCap;
+  int resume;                // 1: continue a partition that yielded
   Control* ctrl;
 };
 
@@ -167,6 +207,38 @@ __device__ __forceinline__ bool grid_barrier(Control* c) {
   return s_err == 0;
 }
 
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Block 0 records a timestamp and a work-item count (phase timeline; read by
+// the host for profiling).  Call right after a grid barrier.
+__device__ __forceinline__ void timeline_mark(Control* c, int info) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const int i = c->tlCount;
+    if (i < kTimeline) {
+      c->tl[i] = global_ns();
+      c->tlInfo[i] = info;
+      c->tlCount = i + 1;
+    }
+  }
+}
+
+// Asynchronous 4-byte global -> shared copy (Ampere+ cp.async); the issuing
+// thread waits for its own copies with cp_async_wait_all().
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
 // Claim the next work item of a phase (CTA-uniform result).
 __device__ __forceinline__ int claim_item(unsigned* ctr) {
   __shared__ int s_item;
@@ -192,6 +264,75 @@ __device__ __forceinline__ void kstore(U* p, long long i, KT v, KT flip) {
 template <typename KT>
 __device__ __forceinline__ int classify(KT k, KT p1, KT p2, KT p3) {
   return (k == p1) ? 1 : (k == p2) ? 3 : (k == p3) ? 5 : (k < p1) ? 0 : (k < p2) ? 2 : (k < p3) ? 4 : 6;
+}
+
+// ---- blocked tile I/O and cheap classification ----
+
+// Thread-blocked chunk of a tile: elements [e0, e0 + kItems) relative to the
+// tile base `tb` (absolute index tbAbs).  16-byte vector loads when the chunk
+// lies inside the array (the tile base is 16-byte aligned because tiles start
+// on absolute multiples of the tile size and the buffers are 16-byte
+// aligned); per-element loads at the array end.  Elements outside [rlo, rhi)
+// are masked out of the returned bit mask.
+template <typename U, typename KT, int kItems>
+__device__ __forceinline__ unsigned load_chunk(const U* tb, long long tbAbs, long long nTotal,
+                                               int e0, int rlo, int rhi, KT flip, KT* key) {
+  constexpr int kBytes = kItems * (int)sizeof(U);
+  static_assert(kBytes % 8 == 0, "chunk must be whole 8-byte vectors");
+  using V = typename std::conditional<kBytes % 16 == 0, uint4, uint2>::type;
+  constexpr int kVec = kBytes / (int)sizeof(V);
+  unsigned ok = 0;
+#pragma unroll
+  for (int i = 0; i < kItems; ++i) ok |= (e0 + i >= rlo && e0 + i < rhi) ? (1u << i) : 0u;
+  if (ok == 0) return 0;
+  if (tbAbs + e0 + kItems <= nTotal) {
+    V v[kVec];
+    const V* src = reinterpret_cast<const V*>(tb + e0);
+#pragma unroll
+    for (int j = 0; j < kVec; ++j) v[j] = src[j];
+    const U* u = reinterpret_cast<const U*>(v);
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) key[i] = KT(u[i]) ^ flip;
+  } else {
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) key[i] = (ok >> i & 1u) ? (KT(tb[e0 + i]) ^ flip) : KT(0);
+  }
+  return ok;
+}
+
+template <int kItems>
+__device__ __forceinline__ void load_ids(const int* tb, long long tbAbs, long long nTotal, int e0,
+                                         unsigned ok, int* id) {
+  static_assert(kItems % 4 == 0, "ids are loaded as int4");
+  if (ok == 0) return;
+  if (tbAbs + e0 + kItems <= nTotal) {
+    const int4* src = reinterpret_cast<const int4*>(tb + e0);
+#pragma unroll
+    for (int j = 0; j < kItems / 4; ++j) {
+      const int4 v = src[j];
+      id[4 * j] = v.x; id[4 * j + 1] = v.y; id[4 * j + 2] = v.z; id[4 * j + 3] = v.w;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) id[i] = (ok >> i & 1u) ? tb[e0 + i] : 0;
+  }
+}
+
+// 7-class code of a key from comparison counts: 2 * #{pivots < k} +
+// #{pivots == k}, remapped through a per-segment table for equal pivots so
+// the classes follow the reference's test order (==p1, ==p2, ==p3 first).
+__device__ __forceinline__ unsigned pivot_lut(bool eq12, bool eq23) {
+  unsigned lut = 0u | 1u << 3 | 2u << 6 | 3u << 9 | 4u << 12 | 5u << 15 | 6u << 18;
+  auto set = [&](int j, unsigned v) { lut = (lut & ~(7u << (3 * j))) | (v << (3 * j)); };
+  if (eq12 && eq23) set(3, 1);
+  else if (eq12) set(2, 1);
+  else if (eq23) set(4, 3);
+  return lut;
+}
+template <typename KT>
+__device__ __forceinline__ int class_lut(KT k, KT p1, KT p2, KT p3, unsigned lut) {
+  const int cp = (k > p1) + (k >= p1) + (k > p2) + (k >= p2) + (k > p3) + (k >= p3);
+  return (int)((lut >> (3 * cp)) & 7u);
 }
 
 // ---- stable one-CTA shared-memory sort ----
@@ -279,6 +420,132 @@ __device__ __forceinline__ void block_sort_groups(KT* sk, int* si, int P) {
     if (kIdx) si[ipad(base + i)] = v[i];
   }
   __syncthreads();
+}
+
+// ---- stable group radix sort (leaves longer than 16 warps' worth of the
+// merge path) ----
+//
+// The CTA's warps are split into groups of Gw warps; group g sorts the n_g
+// elements at smem[g*Gw*32*kItems ...] in place.  Keys are first reduced to
+// (key - min) over the group, so only the bits that differ inside the leaf are
+// sorted (3 eight-bit passes for a typical 32-bit leaf, 1 for bytes).  Each
+// pass is a stable counting scatter: elements are ranked per warp in memory
+// order (warp chunk, round, lane) with __match_any_sync, per-warp digit
+// counters are scanned digit-major inside the group, and every element is
+// written to its new slot.  All threads of the CTA must call it.
+template <typename KT, int kItems, bool kIdx, int NW>
+__device__ __forceinline__ void group_radix_sort(KT* sk, int* si, int n_mine, int Gw,
+                                                 int* cnt /* NW*256 + NW ints */,
+                                                 KT* sred /* 2*NW */, int* spass) {
+  constexpr int kWCH = 32 * kItems;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int g = warp / Gw, wg = warp - g * Gw;  // group, warp inside the group
+  const int gbase = g * Gw * kWCH;              // first element of the group
+  const int wbase = gbase + wg * kWCH;          // first element of this warp
+  unsigned lt;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+  // 1. min / max over the group
+  KT mn = key_max<KT>(), mx = KT(0);
+  for (int r = 0; r < kItems; ++r) {
+    const int e = wg * kWCH + r * 32 + lane;
+    if (e < n_mine) {
+      const KT k = sk[kpad<KT>(gbase + e)];
+      mn = k < mn ? k : mn;
+      mx = k > mx ? k : mx;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const KT a = __shfl_xor_sync(0xffffffffu, mn, o);
+    const KT b = __shfl_xor_sync(0xffffffffu, mx, o);
+    mn = a < mn ? a : mn;
+    mx = b > mx ? b : mx;
+  }
+  if (tid == 0) *spass = 0;
+  if (lane == 0) { sred[warp] = mn; sred[NW + warp] = mx; }
+  __syncthreads();
+  mn = key_max<KT>();
+  mx = KT(0);
+  for (int w = 0; w < Gw; ++w) {
+    const KT a = sred[g * Gw + w], b = sred[NW + g * Gw + w];
+    mn = a < mn ? a : mn;
+    mx = b > mx ? b : mx;
+  }
+  const KT range = (n_mine > 1 && mx > mn) ? KT(mx - mn) : KT(0);
+  int bits = 0;
+  if (range) bits = (sizeof(KT) == 8) ? 64 - __clzll((unsigned long long)range) : 32 - __clz((unsigned)range);
+  const int passes = (bits + 7) >> 3;
+  if (lane == 0 && wg == 0) atomicMax(spass, passes);
+  __syncthreads();
+  const int maxPasses = *spass;
+  int* gcnt = cnt + g * Gw * 256;  // this group's counters, [digit][warp in group]
+  for (int p = 0; p < maxPasses; ++p) {
+    const int shift = p * 8;
+    const bool active = p < passes;
+    // zero the group's counters (each thread: 8 entries)
+    for (int j = (tid - g * Gw * 32); j < Gw * 256; j += Gw * 32) gcnt[j] = 0;
+    KT key[kItems];
+    int id[kItems];
+    unsigned short rk[kItems];
+#pragma unroll
+    for (int r = 0; r < kItems; ++r) {
+      const int e = wg * kWCH + r * 32 + lane;
+      const bool ok = active && e < n_mine;
+      key[r] = ok ? sk[kpad<KT>(gbase + e)] : KT(0);
+      if (kIdx) id[r] = ok ? si[ipad(gbase + e)] : 0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kItems; ++r) {
+      const int e = wg * kWCH + r * 32 + lane;
+      const bool ok = active && e < n_mine;
+      const int d = ok ? (int)(((key[r] - mn) >> shift) & KT(0xff)) : 256 + lane;
+      const unsigned peers = __match_any_sync(0xffffffffu, d);
+      int run = 0;
+      if (ok) run = gcnt[d * Gw + wg];
+      rk[r] = (unsigned short)(run + __popc(peers & lt));
+      __syncwarp();
+      if (ok && (peers >> lane) == 1u) gcnt[d * Gw + wg] = run + __popc(peers);
+      __syncwarp();
+    }
+    __syncthreads();
+    // exclusive scan of the group's 256*Gw counters (digit-major)
+    {
+      const int gt = tid - g * Gw * 32;  // thread index inside the group
+      const int per = 8;                 // 256*Gw / (32*Gw)
+      int v[per];
+      int s = 0;
+#pragma unroll
+      for (int j = 0; j < per; ++j) { v[j] = gcnt[gt * per + j]; s += v[j]; }
+      int inc = s;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+      }
+      __syncthreads();
+      int* wtot = cnt + NW * 256;        // NW spare ints after the counters
+      if (lane == 31) wtot[warp] = inc;
+      __syncthreads();
+      int pre = 0;
+      for (int w = g * Gw; w < warp; ++w) pre += wtot[w];
+      int run = pre + inc - s;
+#pragma unroll
+      for (int j = 0; j < per; ++j) { gcnt[gt * per + j] = run; run += v[j]; }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kItems; ++r) {
+      const int e = wg * kWCH + r * 32 + lane;
+      if (active && e < n_mine) {
+        const int d = (int)(((key[r] - mn) >> shift) & KT(0xff));
+        const int pos = gcnt[d * Gw + wg] + rk[r];
+        sk[kpad<KT>(gbase + pos)] = key[r];
+        if (kIdx) si[ipad(gbase + pos)] = id[r];
+      }
+    }
+    __syncthreads();
+  }
 }
 
 // Size class of a leaf: the smallest power-of-two thread group whose

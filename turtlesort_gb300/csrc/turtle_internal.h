@@ -18,6 +18,7 @@ cudaError_t kernels_launch_multisort(int width, bool hasIdx, void* keys, int* id
                                      long long numArrays, int arrSize, unsigned long long flip,
                                      cudaStream_t stream);
 int kernels_tile_elems(int width);
+int kernels_leaf_max(int width);
 
 // ---- device buffers on the driver VMM API (turtle_vmm.cu) ----
 // Replaces TurtleBuffer::Buffer (turtle-buffer.cuh:7-100) and
