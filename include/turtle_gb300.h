@@ -123,6 +123,26 @@ turtle_status turtle_multisort_device(turtle_sorter* s, void* d_keys, int32_t* d
  * (TURTLE_OK, TURTLE_ERR_TIMEOUT, TURTLE_ERR_CAPACITY). */
 turtle_status turtle_stream_status(turtle_sorter* s, void* stream);
 
+/* Allocation-free sort (no counterpart in the reference): for callers that
+ * may not allocate device memory when they sort -- hosts that own a fixed
+ * device-memory pool and forbid allocations after start-up, plugins handed
+ * device pointers but no allocator, real-time loops that must not block on
+ * the allocator.  Sorts n keys (and ids, or NULL) already in device memory, in
+ * place, on `stream` (NULL = the legacy default stream), using only a 16 MiB
+ * scratch array compiled into the library (held by every GPU that loads the
+ * library until exit).  n must not exceed turtle_noalloc_max_elements()
+ * (1,048,576), else TURTLE_ERR_TOO_LARGE; pointers must be 16-byte aligned.
+ * All calls share the scratch array: calls whose work overlaps on the GPU
+ * race and corrupt each other.  The first call on a device looks up the
+ * array's address and prepares the kernels; make it before any stream
+ * capture.  Waits for `stream` and returns the device-side status.  Calls no
+ * allocating routine. */
+turtle_status turtle_sort_device_noalloc(turtle_dtype dtype, void* d_keys, int32_t* d_idx,
+                                         int64_t n, void* stream);
+
+/* Largest n accepted by turtle_sort_device_noalloc. */
+int64_t turtle_noalloc_max_elements(void);
+
 /* ---- introspection ---- */
 
 /* Kernel launches issued by this sorter since it was created. */

@@ -52,6 +52,8 @@ SIGNATURES = [
     ("turtle_debug_fail_allocations", None, [_I]),
     ("turtle_version", C.c_char_p, []),
     ("turtle_debug_timeline", _I, [_P, _P, _P, _I]),
+    ("turtle_sort_device_noalloc", _I, [_I, _P, _P, _I64, _P]),
+    ("turtle_noalloc_max_elements", _I64, []),
 ]
 
 _lib = None

@@ -19,68 +19,15 @@
 #include "../../include/turtle_gb300.h"
 #include "turtle_device.cuh"
 #include "turtle_internal.h"
+#include "turtle_layout.cuh"
 
 using turtle::DevBuffer;
+using turtle::WsLayout;
+using turtle::make_layout;
+using turtle::dtype_width;
+using turtle::dtype_flip;
 
 namespace {
-
-struct WsLayout {
-  int segCap = 0, tileCap = 0, leafCap = 0, fillCap = 0;
-  size_t offWarpCnt[2] = {0, 0};
-  size_t offCtrl = 0, offSegs[2] = {0, 0}, offTiles[2] = {0, 0}, offTileCnt[2] = {0, 0},
-         offTileOff[2] = {0, 0};
-  size_t offLeaves = 0, offLeavesSorted = 0, offFills = 0, bytes = 0;
-};
-
-size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
-
-WsLayout make_layout(long long maxN, int tile, int leafMax, long long extraLeaves) {
-  WsLayout L;
-  // segments of one level are disjoint and longer than leafMax
-  const long long segCap = maxN / leafMax + 66;
-  const long long tileCap = maxN / tile + 2 * segCap + 64;
-  // leaf / fill lists: roomy enough that a partition never has to yield on
-  // ordinary inputs (one level adds at most 4 leaves and 3 fills per segment)
-  const long long leafCap = std::max(8 * (segCap + 1), maxN / 64) + extraLeaves + 4096;
-  const long long fillCap = 2 * (3 * (segCap + 1) + tileCap) + maxN / 64 + 4096;
-  L.segCap = (int)segCap;
-  L.tileCap = (int)tileCap;
-  L.leafCap = (int)leafCap;
-  L.fillCap = (int)fillCap;
-  size_t o = 0;
-  L.offCtrl = o; o = align_up(o + sizeof(turtle::Control), 256);
-  for (int p = 0; p < 2; ++p) { L.offSegs[p] = o; o = align_up(o + segCap * sizeof(turtle::SegDesc), 256); }
-  for (int p = 0; p < 2; ++p) { L.offTiles[p] = o; o = align_up(o + tileCap * sizeof(turtle::TileDesc), 256); }
-  for (int p = 0; p < 2; ++p) { L.offTileCnt[p] = o; o = align_up(o + tileCap * 8 * sizeof(int), 256); }
-  for (int p = 0; p < 2; ++p) { L.offTileOff[p] = o; o = align_up(o + tileCap * 8 * sizeof(long long), 256); }
-  // per-warp-chunk counts: kThreads / 32 chunks per tile (the partition CTA's warps)
-  for (int p = 0; p < 2; ++p) { L.offWarpCnt[p] = o; o = align_up(o + tileCap * 16 * 8 * sizeof(int), 256); }
-  L.offLeaves = o; o = align_up(o + leafCap * sizeof(turtle::LeafDesc), 256);
-  L.offLeavesSorted = o; o = align_up(o + leafCap * sizeof(turtle::LeafDesc), 256);
-  L.offFills = o; o = align_up(o + fillCap * sizeof(turtle::FillDesc), 256);
-  L.bytes = o;
-  return L;
-}
-
-int dtype_width(int dt) {
-  switch (dt) {
-    case TURTLE_INT8: case TURTLE_UINT8: return 1;
-    case TURTLE_INT16: case TURTLE_UINT16: return 2;
-    case TURTLE_INT32: case TURTLE_UINT32: return 4;
-    case TURTLE_INT64: case TURTLE_UINT64: return 8;
-    default: return 0;
-  }
-}
-
-unsigned long long dtype_flip(int dt) {
-  switch (dt) {
-    case TURTLE_INT8: return 0x80ull;
-    case TURTLE_INT16: return 0x8000ull;
-    case TURTLE_INT32: return 0x80000000ull;
-    case TURTLE_INT64: return 0x8000000000000000ull;
-    default: return 0ull;
-  }
-}
 
 constexpr long long kMaxElements = (1LL << 31) - 1;  // int32 ids and in-segment offsets
 
@@ -153,33 +100,8 @@ turtle_status alloc_workspace(turtle_sorter* s, long long extraLeaves) {
 
 turtle::SortArgs make_args(turtle_sorter* s, void* keys, int32_t* idx, const long long* offs,
                            long long num, long long n) {
-  turtle::SortArgs a;
-  std::memset(&a, 0, sizeof(a));
-  char* w = (char*)s->ws.ptr;
-  a.keysA = keys;
-  a.idxA = idx;
-  a.keysB = s->keysB.ptr;
-  a.idxB = (int*)s->idxB.ptr;
-  a.offsets = offs;
-  a.numArrays = num;
-  a.n = n;
-  a.flip = s->flip;
-  for (int p = 0; p < 2; ++p) {
-    a.segs[p] = (turtle::SegDesc*)(w + s->lay.offSegs[p]);
-    a.tiles[p] = (turtle::TileDesc*)(w + s->lay.offTiles[p]);
-    a.tileCnt[p] = (int*)(w + s->lay.offTileCnt[p]);
-    a.warpCnt[p] = (int*)(w + s->lay.offWarpCnt[p]);
-    a.tileOff[p] = (long long*)(w + s->lay.offTileOff[p]);
-  }
-  a.leaves = (turtle::LeafDesc*)(w + s->lay.offLeaves);
-  a.leavesSorted = (turtle::LeafDesc*)(w + s->lay.offLeavesSorted);
-  a.fills = (turtle::FillDesc*)(w + s->lay.offFills);
-  a.segCap = s->lay.segCap;
-  a.tileCap = s->lay.tileCap;
-  a.leafCap = s->lay.leafCap;
-  a.fillCap = s->lay.fillCap;
-  a.ctrl = (turtle::Control*)(w + s->lay.offCtrl);
-  return a;
+  return turtle::bind_args(keys, idx, s->keysB.ptr, (int*)s->idxB.ptr, (char*)s->ws.ptr, s->lay,
+                           offs, num, n, s->flip);
 }
 
 // Enqueue: reset the control block, run the persistent kernel, copy the
