@@ -143,6 +143,59 @@ turtle_status turtle_sort_device_noalloc(turtle_dtype dtype, void* d_keys, int32
 /* Largest n accepted by turtle_sort_device_noalloc. */
 int64_t turtle_noalloc_max_elements(void);
 
+/* ---- serving loop: continuous batching (no reference counterpart) ----
+ *
+ * The reference sorts one array per StartSorting/Sync pair on one host thread
+ * (turtle-sort.cuh:124-258); a serving process calls it once per request,
+ * serially.  A turtle_server takes requests of any of the eight dtypes, with
+ * or without ids, from any host thread.  A scheduler thread admits waiting
+ * requests in arrival order while their device memory fits the HBM budget,
+ * fuses consecutive requests of the same (dtype, ids) group into one batched
+ * persistent launch, and keeps up to three batches in flight (copy in, sort,
+ * copy out overlap on separate streams).  Results are identical to sorting
+ * each request alone. */
+typedef struct turtle_server turtle_server; /* opaque */
+
+typedef struct turtle_server_stats {
+  int64_t submitted, completed, failed, batches;
+  int64_t keys;          /* keys of completed requests */
+  double p50_ms, p99_ms, mean_ms, max_ms; /* submit -> done latency */
+  double span_s;         /* first submit -> last completion */
+  double keys_per_s;     /* keys / span_s */
+  int64_t in_use_bytes;  /* device bytes held by batches in flight */
+} turtle_server_stats;
+
+/* Starts a server on `device` (< 0: current) that holds at most
+ * hbm_budget_bytes of device memory for batches in flight.  A batch fuses at
+ * most max_batch_requests requests (<= 0: 4096) and max_batch_keys keys
+ * (<= 0: 2^25; a single larger request forms a batch alone). */
+turtle_status turtle_server_create(int device, int64_t hbm_budget_bytes, int max_batch_requests,
+                                   int64_t max_batch_keys, turtle_server** out);
+
+/* Queues a sort of n keys at host_keys (and n int32 ids at host_idx, or NULL)
+ * in place.  Host buffers should be pinned for full copy speed and must stay
+ * valid until turtle_server_wait returns for the ticket.  A request whose
+ * batch can never fit the budget completes with TURTLE_ERR_BUDGET. */
+turtle_status turtle_server_submit(turtle_server* srv, turtle_dtype dtype, void* host_keys,
+                                   int32_t* host_idx, int64_t n, uint64_t* ticket);
+
+/* *done = 1 when the request has finished (results are in its buffers). */
+turtle_status turtle_server_poll(turtle_server* srv, uint64_t ticket, int* done);
+
+/* Blocks until the request has finished, stores its submit-to-done latency
+ * (may be NULL), releases the ticket and returns the request's status. */
+turtle_status turtle_server_wait(turtle_server* srv, uint64_t ticket, double* latency_seconds);
+
+/* Blocks until no request is waiting or in flight. */
+turtle_status turtle_server_drain(turtle_server* srv);
+
+/* Counters and latency percentiles of the completed requests. */
+turtle_status turtle_server_get_stats(turtle_server* srv, turtle_server_stats* out);
+
+/* Finishes every queued request, then stops the scheduler thread and frees
+ * the server.  Safe on NULL. */
+turtle_status turtle_server_destroy(turtle_server* srv);
+
 /* ---- introspection ---- */
 
 /* Kernel launches issued by this sorter since it was created. */

@@ -71,3 +71,16 @@ def test_python_mirror_raises_without_device(native_lib):
     with pytest.raises(TurtleError) as e:
         TurtleSort(np.int32, 1000)
     assert e.value.status == 9
+
+
+def test_server_host_side_checks(native_lib):
+    h = C.c_void_p()
+    assert native_lib.turtle_server_create(-1, 0, 0, 0, C.byref(h)) == 1  # no budget
+    assert native_lib.turtle_server_create(-1, 1 << 30, 0, 0, None) == 1
+    assert native_lib.turtle_server_destroy(None) == 0
+    t = C.c_uint64()
+    assert native_lib.turtle_server_submit(None, 4, None, None, 0, C.byref(t)) == 1
+    assert native_lib.turtle_server_drain(None) == 1
+    if not has_gpu():
+        assert native_lib.turtle_server_create(-1, 1 << 30, 0, 0, C.byref(h)) == 9
+        assert not h.value

@@ -22,7 +22,8 @@ import numpy as np
 from . import _native
 from ._native import TurtleError
 
-__all__ = ["TurtleSort", "TurtleError", "dtype_code", "smem_capacity", "load_library"]
+__all__ = ["TurtleSort", "TurtleServer", "TurtleError", "dtype_code", "smem_capacity",
+           "load_library"]
 
 _DTYPES = {
     np.dtype(np.int8): _native.INT8,
@@ -201,3 +202,80 @@ class TurtleSort:
     @property
     def last_levels(self) -> int:
         return int(self._lib.turtle_last_levels(self._h))
+
+
+class TurtleServer:
+    """Continuous-batching sort server over the C ABI (turtle_server_*).
+
+    No reference counterpart: a serving process on the reference issues one
+    StartSorting/Sync pair per request (turtle-sort.cuh:124-258).  Requests are
+    numpy arrays sorted in place; submit() returns a ticket, wait() blocks on
+    it.  Arrays should live in pinned memory for full copy speed (any host
+    memory works) and must stay alive until wait() returns.
+    """
+
+    def __init__(self, hbm_budget_bytes: int, device: int = -1, max_batch_requests: int = 0,
+                 max_batch_keys: int = 0):
+        self._lib = load_library()
+        h = C.c_void_p()
+        st = self._lib.turtle_server_create(int(device), int(hbm_budget_bytes),
+                                            int(max_batch_requests), int(max_batch_keys),
+                                            C.byref(h))
+        _check(st, "turtle_server_create")
+        self._h = h
+        self._keep = {}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.turtle_server_destroy(self._h)
+            self._h = None
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, values: np.ndarray, index: Optional[np.ndarray] = None) -> int:
+        if not values.flags.c_contiguous:
+            raise ValueError("values must be C-contiguous")
+        if index is not None:
+            if index.dtype != np.int32 or index.shape != values.shape or not index.flags.c_contiguous:
+                raise ValueError("index must be a C-contiguous int32 array of the values' shape")
+        t = C.c_uint64()
+        st = self._lib.turtle_server_submit(
+            self._h, dtype_code(values.dtype), values.ctypes.data_as(C.c_void_p),
+            index.ctypes.data_as(C.c_void_p) if index is not None else None, int(values.size),
+            C.byref(t))
+        _check(st, "turtle_server_submit")
+        self._keep[t.value] = (values, index)
+        return int(t.value)
+
+    def poll(self, ticket: int) -> bool:
+        d = C.c_int()
+        _check(self._lib.turtle_server_poll(self._h, C.c_uint64(ticket), C.byref(d)),
+               "turtle_server_poll")
+        return bool(d.value)
+
+    def wait(self, ticket: int) -> float:
+        """Blocks until the request is sorted; returns its latency in seconds."""
+        lat = C.c_double()
+        st = self._lib.turtle_server_wait(self._h, C.c_uint64(ticket), C.byref(lat))
+        self._keep.pop(ticket, None)
+        _check(st, "turtle_server_wait")
+        return float(lat.value)
+
+    def drain(self) -> None:
+        _check(self._lib.turtle_server_drain(self._h), "turtle_server_drain")
+
+    def stats(self) -> dict:
+        s = _native.ServerStats()
+        _check(self._lib.turtle_server_get_stats(self._h, C.byref(s)), "turtle_server_get_stats")
+        return {name: getattr(s, name) for name, _ in s._fields_}

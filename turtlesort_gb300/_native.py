@@ -54,7 +54,26 @@ SIGNATURES = [
     ("turtle_debug_timeline", _I, [_P, _P, _P, _I]),
     ("turtle_sort_device_noalloc", _I, [_I, _P, _P, _I64, _P]),
     ("turtle_noalloc_max_elements", _I64, []),
+    ("turtle_server_create", _I, [_I, _I64, _I, _I64, C.POINTER(_P)]),
+    ("turtle_server_submit", _I, [_P, _I, _P, _P, _I64, C.POINTER(C.c_uint64)]),
+    ("turtle_server_poll", _I, [_P, C.c_uint64, C.POINTER(_I)]),
+    ("turtle_server_wait", _I, [_P, C.c_uint64, C.POINTER(C.c_double)]),
+    ("turtle_server_drain", _I, [_P]),
+    ("turtle_server_get_stats", _I, [_P, _P]),
+    ("turtle_server_destroy", _I, [_P]),
 ]
+
+
+class ServerStats(C.Structure):
+    """turtle_server_stats of include/turtle_gb300.h."""
+
+    _fields_ = [
+        ("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64),
+        ("batches", C.c_int64), ("keys", C.c_int64),
+        ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("mean_ms", C.c_double),
+        ("max_ms", C.c_double), ("span_s", C.c_double), ("keys_per_s", C.c_double),
+        ("in_use_bytes", C.c_int64),
+    ]
 
 _lib = None
 
