@@ -52,15 +52,20 @@ def peaks() -> tuple[float, str]:
     return 6800.0, "fallback"
 
 
-def profile_traffic() -> float | None:
-    """DRAM bytes per launch of the persistent kernel from the committed ncu
-    summary (profiles/persistent_sort_traffic.json), if present."""
-    p = ROOT / "profiles" / "persistent_sort_traffic.json"
-    if p.exists():
-        try:
-            return float(json.loads(p.read_text())["dram_bytes_per_launch_64M_int32_idx"])
-        except Exception:
-            return None
+def profile_traffic(n: int) -> float | None:
+    """DRAM bytes (read + write) per launch of the persistent kernel, from the
+    committed ncu summary of that kernel (the line
+    `traffic_bytes_per_launch_2^26: B`), for the 2^26-element workload only."""
+    p = ROOT / "profiles" / "persistent_sort_kernel_32M_int32_idx.md"
+    if n != 1 << 26 or not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        line = line.strip()
+        if line.startswith("traffic_bytes_per_launch_2^26:"):
+            try:
+                return float(line.split(":", 1)[1])
+            except ValueError:
+                return None
     return None
 
 
@@ -278,7 +283,7 @@ def run_gpu(args) -> None:
     peak, peak_kind = peaks()
     alg_bytes = 4.0 * n * (4 + 4)
     achieved = alg_bytes / (ms_step / 1e3) / 1e9
-    traffic = profile_traffic()
+    traffic = profile_traffic(n)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
