@@ -19,9 +19,16 @@
 
 namespace turtle {
 
-constexpr int kThreads = 512;            // CTA size of the partition kernel
+#ifndef TURTLE_PART_THREADS
+#define TURTLE_PART_THREADS 768
+#endif
+#ifndef TURTLE_PART_BLOCKS
+#define TURTLE_PART_BLOCKS 1
+#endif
+constexpr int kThreads = TURTLE_PART_THREADS;  // CTA size of the partition kernel
 constexpr int kWarps = kThreads / 32;
-constexpr int kMinBlocks = 2;            // resident partition CTAs per SM we compile for
+constexpr int kMinBlocks = TURTLE_PART_BLOCKS; // resident partition CTAs per SM we compile for
+constexpr int kPartTile = 4096;          // partition tile (keys), a power of two
 constexpr int kLThreads = 512;           // CTA size of the leaf / batched kernels
 constexpr int kLWarps = kLThreads / 32;
 constexpr int kFillChunk = 1 << 16;      // pivot-run fill work unit (elements)
@@ -45,20 +52,17 @@ template <typename U> struct KeyCfg;
 template <> struct KeyCfg<uint8_t> { using KT = uint32_t; static constexpr int kItems = 8, kLItems = 16; };
 template <> struct KeyCfg<uint16_t> { using KT = uint32_t; static constexpr int kItems = 8, kLItems = 16; };
 template <> struct KeyCfg<uint32_t> { using KT = uint32_t; static constexpr int kItems = 8, kLItems = 16; };
-template <> struct KeyCfg<uint64_t> { using KT = uint64_t; static constexpr int kItems = 8, kLItems = 8; };
+template <> struct KeyCfg<uint64_t> { using KT = uint64_t; static constexpr int kItems = 4, kLItems = 8; };
 
 template <typename U>
 struct Geom {
   using KT = typename KeyCfg<U>::KT;
   static constexpr int kItems = KeyCfg<U>::kItems;
   static constexpr int kLItems = KeyCfg<U>::kLItems;
-  static constexpr int kTile = kThreads * kItems;       // partition tile
+  static constexpr int kTile = kPartTile;               // partition tile
   static constexpr int kLeafMax = kLThreads * kLItems;  // shared-memory sort capacity
   static constexpr int kWarpChunk = 32 * kItems;        // elements per warp chunk
-  static constexpr int kChunks = kTile / kWarpChunk;    // warp chunks per tile
   static constexpr int kKeyPadShift = sizeof(KT) == 8 ? 4 : 5;
-  static constexpr int kKeySlots = kTile + (kTile >> kKeyPadShift) + 8;
-  static constexpr int kIdxSlots = kTile + (kTile >> 5) + 8;
   static constexpr int kLeafKeySlots = kLeafMax + (kLeafMax >> kKeyPadShift) + 8;
   static constexpr int kLeafIdxSlots = kLeafMax + (kLeafMax >> 5) + 8;
 };
@@ -81,15 +85,13 @@ struct SegDesc {        // a segment partitioned by the multi-CTA 3-pivot pass
   long long n;
   int tileBase;         // first entry in this level's tile arrays
   int ntiles;
-  int done;             // count-phase tiles finished (last one plans)
-  int pad;
-  unsigned long long piv[3];  // pivot candidates a[start+n/2], a[start], a[stop]
-                              // (unsigned images; captured by the parent's scatter)
-  long long cbase[8];   // class boundaries after planning (cbase[7] = end)
-  int childSeg[4];      // next-level segment of classes 0,2,4,6 (-1: none)
+  unsigned long long piv[3];   // pivot candidates a[start+n/2], a[start], a[stop]
+                               // (unsigned images; captured by the parent's scatter)
   unsigned long long pivS[3];  // sorted pivots (unsigned images), set by the plan
   unsigned lut;         // class remap for equal pivots, set by the plan
-  int pad2;
+  int pad;
+  long long cbase[8];   // class boundaries after planning (cbase[7] = end)
+  int childSeg[4];      // next-level segment of classes 0,2,4,6 (-1: none)
 };
 struct TileDesc {       // one partition tile: [lo, hi) of segment seg
   long long lo;
@@ -147,8 +149,8 @@ struct SortArgs {
   unsigned long long flip;   // sign-bit mask for signed dtypes (0 otherwise)
   SegDesc* segs[2];
   TileDesc* tiles[2];
-  int* tileCnt[2];           // [tile][8] class counts (summed over the tile's warps)
-  int* warpCnt[2];           // [tile][kChunks][8] class counts per warp chunk
+  int* tileCnt[2];           // [tile][8]: #(k<p1), #(k<=p1), #(k<p2), #(k<=p2), #(k<p3),
+                             // #(k<=p3), #keys (predicate totals against the segment's pivots)
   long long* tileOff[2];     // [tile][8] global destination of each class
   LeafDesc* leaves;
   LeafDesc* leavesSorted;
@@ -239,6 +241,58 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
 
+// ---- bulk asynchronous copies (TMA, non-tensor form) with an mbarrier ----
+// One warp-private mbarrier tracks the bulk copies of one chunk: lane 0 arms it
+// with the byte count and issues the copies; every lane then waits for the
+// phase flip.  Both addresses and the size of a bulk copy must be multiples of
+// 16 bytes; callers check this and fall back to plain loads otherwise.
+constexpr long long kTmaSpinLimit = 1LL << 22;  // bounded mbarrier polls
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* m, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(m)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+// Orders this thread's earlier generic-proxy accesses (shared and global)
+// before its later bulk copies: the copies read global data that other CTAs
+// wrote before the last grid barrier and overwrite shared bytes this warp has
+// just read.
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async;\n" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arm(unsigned long long* m, unsigned bytes) {
+  asm volatile(
+      "{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}\n" ::"r"(
+          smem_u32(m)),
+      "r"(bytes)
+      : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes,
+                                         unsigned long long* m) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(m))
+      : "memory");
+}
+// Bounded wait for phase `parity` of the mbarrier; false after kTmaSpinLimit polls.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* m, unsigned parity) {
+  const unsigned a = smem_u32(m);
+  for (long long it = 0; it < kTmaSpinLimit; ++it) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
 // Claim the next work item of a phase (CTA-uniform result).
 __device__ __forceinline__ int claim_item(unsigned* ctr) {
   __shared__ int s_item;
@@ -289,13 +343,13 @@ __device__ __forceinline__ unsigned load_chunk(const U* tb, long long tbAbs, lon
     V v[kVec];
     const V* src = reinterpret_cast<const V*>(tb + e0);
 #pragma unroll
-    for (int j = 0; j < kVec; ++j) v[j] = src[j];
+    for (int j = 0; j < kVec; ++j) v[j] = __ldcg(src + j);
     const U* u = reinterpret_cast<const U*>(v);
 #pragma unroll
     for (int i = 0; i < kItems; ++i) key[i] = KT(u[i]) ^ flip;
   } else {
 #pragma unroll
-    for (int i = 0; i < kItems; ++i) key[i] = (ok >> i & 1u) ? (KT(tb[e0 + i]) ^ flip) : KT(0);
+    for (int i = 0; i < kItems; ++i) key[i] = (ok >> i & 1u) ? (KT(__ldcg(tb + e0 + i)) ^ flip) : KT(0);
   }
   return ok;
 }
@@ -309,12 +363,12 @@ __device__ __forceinline__ void load_ids(const int* tb, long long tbAbs, long lo
     const int4* src = reinterpret_cast<const int4*>(tb + e0);
 #pragma unroll
     for (int j = 0; j < kItems / 4; ++j) {
-      const int4 v = src[j];
+      const int4 v = __ldcg(src + j);
       id[4 * j] = v.x; id[4 * j + 1] = v.y; id[4 * j + 2] = v.z; id[4 * j + 3] = v.w;
     }
   } else {
 #pragma unroll
-    for (int i = 0; i < kItems; ++i) id[i] = (ok >> i & 1u) ? tb[e0 + i] : 0;
+    for (int i = 0; i < kItems; ++i) id[i] = (ok >> i & 1u) ? __ldcg(tb + e0 + i) : 0;
   }
 }
 

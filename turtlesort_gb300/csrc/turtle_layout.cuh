@@ -14,7 +14,6 @@ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 struct WsLayout {
   int segCap = 0, tileCap = 0, leafCap = 0, fillCap = 0;
-  size_t offWarpCnt[2] = {0, 0};
   size_t offCtrl = 0, offSegs[2] = {0, 0}, offTiles[2] = {0, 0}, offTileCnt[2] = {0, 0},
          offTileOff[2] = {0, 0};
   size_t offLeaves = 0, offLeavesSorted = 0, offFills = 0, bytes = 0;
@@ -39,8 +38,6 @@ inline WsLayout make_layout(long long maxN, int tile, int leafMax, long long ext
   for (int p = 0; p < 2; ++p) { L.offTiles[p] = o; o = align_up(o + tileCap * sizeof(turtle::TileDesc), 256); }
   for (int p = 0; p < 2; ++p) { L.offTileCnt[p] = o; o = align_up(o + tileCap * 8 * sizeof(int), 256); }
   for (int p = 0; p < 2; ++p) { L.offTileOff[p] = o; o = align_up(o + tileCap * 8 * sizeof(long long), 256); }
-  // per-warp-chunk counts: kThreads / 32 chunks per tile (the partition CTA's warps)
-  for (int p = 0; p < 2; ++p) { L.offWarpCnt[p] = o; o = align_up(o + tileCap * 16 * 8 * sizeof(int), 256); }
   L.offLeaves = o; o = align_up(o + leafCap * sizeof(turtle::LeafDesc), 256);
   L.offLeavesSorted = o; o = align_up(o + leafCap * sizeof(turtle::LeafDesc), 256);
   L.offFills = o; o = align_up(o + fillCap * sizeof(turtle::FillDesc), 256);
@@ -88,7 +85,6 @@ inline SortArgs bind_args(void* keys, int* idx, void* keysB, int* idxB, char* ws
     a.tiles[p] = (TileDesc*)(ws + L.offTiles[p]);
     a.tileCnt[p] = (int*)(ws + L.offTileCnt[p]);
     a.tileOff[p] = (long long*)(ws + L.offTileOff[p]);
-    a.warpCnt[p] = (int*)(ws + L.offWarpCnt[p]);
   }
   a.leaves = (LeafDesc*)(ws + L.offLeaves);
   a.leavesSorted = (LeafDesc*)(ws + L.offLeavesSorted);

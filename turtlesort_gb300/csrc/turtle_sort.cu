@@ -3,35 +3,39 @@
 //
 // persistent_sort_kernel (replaces the CDP2 chain copyTasksBack ->
 // resetNumTasks -> quickSortWithoutStreamCompaction / bruteSort,
-// turtle-sort.cu:35-188,573-934): one cooperative launch of (SMs x 2) blocks
-// walks the partition tree level by level.  Every level has two phases
+// turtle-sort.cu:35-188,573-934): one cooperative launch of one CTA per SM
+// walks the partition tree level by level.  Every level has three phases
 // separated by a bounded grid barrier:
-//   COUNT   each tile (kTile elements of one segment, aligned to absolute
-//           kTile boundaries) counts its keys against the segment's pivots;
-//           the CTA that completes a segment's last tile plans it: per-class
-//           totals, per-tile destination offsets and the children
-//           (next-level segments with their tile descriptors, leaves, parked
-//           pivot runs).
-//   SCATTER each tile re-reads its keys (+ids), ranks them stably per class
-//           (thread-local counts + one block scan), stages them by class in
-//           shared memory and writes each class run coalesced to its
-//           destination in the other buffer.  Pivot runs are written by value
-//           and never recursed into.  The tile that writes a child's first,
-//           middle or last element records it in the child's descriptor:
-//           those are the child's pivots.
+//   COUNT   one warp per tile (kTile keys of one segment, aligned to absolute
+//           kTile boundaries) counts its keys against the segment's pivots
+//           (six predicate totals).
+//   PLAN    one CTA per segment turns the per-tile totals into class totals
+//           and per-tile destination offsets (class order as in
+//           turtle-sort.cu:755-761, then tiles in memory order: stable) and
+//           routes the children (next-level segments with their tiles,
+//           leaves, parked pivot runs; turtle-sort.cu:857-933).
+//   SCATTER one warp per tile, 256-key chunks prefetched into shared memory
+//           by bulk asynchronous copies (TMA).  Per chunk the warp ranks the
+//           keys stably per class (4-bit per-lane counters, one warp scan),
+//           stages them by class in shared memory and writes each class run
+//           coalesced to its destination in the other buffer.  Pivot runs are
+//           written by value and never recursed into.  The warp whose chunk
+//           holds a child's first, middle or last key reads it from the stage
+//           and records it: those three keys are the child's pivots.
 // Children live in the other buffer (ping-pong A <-> B), so there is no
 // copy-back pass.  At the end the kernel buckets the leaves by size and hands
-// them to leaf_kernel, which sorts them in shared memory (short leaves with the
-// register network + merge-path merge, long ones with the stable radix groups)
-// and fills the parked pivot runs.  If the leaf lists would overflow before
-// the tree is done (pathological inputs only), the kernel yields: the host
-// runs leaf_kernel and relaunches the partition from the saved level.
+// them to leaf_kernel, which sorts them in shared memory (register network +
+// merge-path merge) and fills the parked pivot runs.  If the leaf lists would
+// overflow before the tree is done (pathological inputs only), the kernel
+// yields: the host runs leaf_kernel and relaunches the partition from the
+// saved level.
 //
 // Pivots are the reference's: sorted{a[start + n/2], a[start], a[stop]}
-// (turtle-sort.cu:641-655).  After kDepthSwitch levels a segment's pivots are
-// the quartiles of 31 evenly spaced samples instead, which bounds the depth on
-// inputs built against median-of-3; the output does not depend on the pivots
-// (every step is stable, so the result equals a stable sort by key).
+// (turtle-sort.cu:641-655).  From kDepthSwitch levels on, a segment's pivots
+// are the quartiles of 31 evenly spaced samples instead, which bounds the
+// depth on inputs built against median-of-3; the output does not depend on
+// the pivots (every step is stable, so the result equals a stable sort by
+// key).
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
@@ -48,7 +52,9 @@ constexpr int kMergeClassMax = 4;
 // The merge-path groups measured faster than the radix groups for every leaf
 // class on GB300, so the radix groups are compiled out of the leaf sort.
 constexpr bool kRadixLeaves = false;
-constexpr int kCountBatch = 8;  // tiles per COUNT work item
+
+constexpr int ilog2(int x) { return x <= 1 ? 0 : 1 + ilog2(x >> 1); }
+constexpr unsigned kFull = 0xffffffffu;
 
 template <typename U, bool kIdx>
 struct Persist {
@@ -56,35 +62,38 @@ struct Persist {
   using KT = typename G::KT;
   static constexpr int kItems = G::kItems;
   static constexpr int kTile = G::kTile;
+  static constexpr int kTileShift = ilog2(kTile);
+  static_assert((1 << kTileShift) == kTile, "tiles are a power of two");
   static constexpr int kLeafMax = G::kLeafMax;
-  static constexpr int kIdxSlots = kIdx ? G::kIdxSlots : 4;
+  static constexpr int kWCH = G::kWarpChunk;
+  static_assert(kWCH == 32 * kItems && kWCH <= 256, "stage slots are 8-bit");
+  static_assert(kItems <= 8, "per-lane class counters are 4-bit");
+
+  // One per warp: the chunk double buffer (bulk-copy destinations), the
+  // class-ordered stage and the warp's destination tables.
+  struct alignas(16) WarpArea {
+    U pk[2][kWCH];                  // raw keys of the chunks in flight
+    int pi[2][kIdx ? kWCH : 4];     // their ids
+    KT sk[kWCH];                    // staged keys (class order)
+    int si[kIdx ? kWCH : 4];        // staged ids
+    unsigned char sc[kWCH];         // class of each stage slot
+    long long delta[8];             // destination minus stage slot, per class
+    long long wbase[8];             // running destination per class
+    long long cpos[12];             // children's pivot positions (-1: none)
+    int cseg[12];                   // the child segment of each position
+    unsigned long long mbar[2];     // bulk-copy completion barriers
+  };
 
   struct Smem {  // partition CTA
-    KT keys[G::kKeySlots];
-    int idx[kIdxSlots];
-    int classStart[8];
-    int cnt[8];
-    long long toff[8];
-    long long red[kWarps][8];
-    long long carry[8];
-    long long tot[8];
-    long long cbase[8];
-    long long ppos[4][3];       // child pivot positions (start+n/2, start, stop)
-    long long dbias[8];         // per-class destination minus stage index
-    unsigned wpred[kWarps][4];  // COUNT: per-warp predicate totals
-    unsigned wscan[kWarps][4];  // SCATTER: per-warp class-count totals
-    long long wbase[kWarps][8];  // SCATTER: per-warp destination base per class
-    unsigned dstRel[kWarps * (32 * kItems + kItems)];  // SCATTER: staged destinations
-    unsigned wpre[kWarps][4];   // SCATTER: exclusive warp prefixes
-    TileDesc tds[kCountBatch];
+    WarpArea w[kWarps];
+    int red[kWarps][8];
+    int tot[8];
+    int cbase[8];                   // class boundaries relative to the segment start
     int childSeg[4];
     int childTb[4], childNt[4];
     long long childStart[4], childN[4];
     KT piv[3];
     unsigned lut;
-    int seg, item, nPlan;
-    int segList[kCountBatch];
-    int planList[kCountBatch];
     int classOff[16];
     int classItems[16];
   };
@@ -130,7 +139,8 @@ template <typename KT, typename U>
 __device__ __noinline__ void sampled_pivots(const U* src, long long start, long long n, KT flip,
                                             KT* piv) {
   KT s[31];
-  for (int i = 0; i < 31; ++i) s[i] = kload<U, KT>(src, start + (n * (2 * i + 1)) / 62, flip);
+  for (int i = 0; i < 31; ++i)
+    s[i] = KT(__ldcg(src + start + (n * (2 * i + 1)) / 62)) ^ flip;
   for (int i = 1; i < 31; ++i) {
     KT x = s[i];
     int j = i - 1;
@@ -140,14 +150,16 @@ __device__ __noinline__ void sampled_pivots(const U* src, long long start, long 
   piv[0] = s[7]; piv[1] = s[15]; piv[2] = s[23];
 }
 
-// Pivots of a segment: the captured candidates, or samples on deep levels.
+// Sorted pivots of a segment: its captured candidates on shallow levels,
+// samples of its keys on deep ones.
 template <typename KT, typename U>
-__device__ __forceinline__ void segment_pivots(const SegDesc& sd, const U* src, int level, KT flip,
+__device__ __forceinline__ void segment_pivots(const SegDesc* sd, const U* src, int level, KT flip,
                                                KT* piv) {
-  if (level < kDepthSwitch)
-    sort3<KT>((KT)__ldcg(&sd.piv[0]), (KT)__ldcg(&sd.piv[1]), (KT)__ldcg(&sd.piv[2]), piv);
-  else
-    sampled_pivots<KT, U>(src, __ldcg(&sd.start), __ldcg(&sd.n), flip, piv);
+  if (level < kDepthSwitch) {
+    sort3<KT>((KT)__ldcg(&sd->piv[0]), (KT)__ldcg(&sd->piv[1]), (KT)__ldcg(&sd->piv[2]), piv);
+  } else {
+    sampled_pivots<KT, U>(src, __ldcg(&sd->start), __ldcg(&sd->n), flip, piv);
+  }
 }
 
 template <int kTile>
@@ -171,8 +183,10 @@ __device__ int alloc_segment(const SortArgs& a, int par, long long start, long l
     return -1;
   }
   SegDesc d;
-  d.start = start; d.n = n; d.tileBase = (int)tb; d.ntiles = (int)nt; d.done = 0; d.pad = 0;
+  d.start = start; d.n = n; d.tileBase = (int)tb; d.ntiles = (int)nt;
   d.piv[0] = d.piv[1] = d.piv[2] = 0;
+  d.pivS[0] = d.pivS[1] = d.pivS[2] = 0;
+  d.lut = 0; d.pad = 0;
   for (int c = 0; c < 8; ++c) d.cbase[c] = 0;
   for (int c = 0; c < 4; ++c) d.childSeg[c] = -1;
   a.segs[par][si] = d;
@@ -229,8 +243,8 @@ __device__ void push_fill(const SortArgs& a, long long start, long long n, unsig
   }
 }
 
-// Route one input array at init: nothing, leaf, or level-0 segment (whose
-// pivots this thread reads, and whose tiles it writes when writeTiles).
+// Route one input array at init: nothing, leaf, or level-0 segment (with its
+// pivot candidates; its tiles are written when writeTiles).
 template <typename U, int kTile, int kLeafMax>
 __device__ void route_input(const SortArgs& a, long long start, long long n, bool writeTiles,
                             int* siOut, int* tbOut, int* ntOut) {
@@ -253,16 +267,11 @@ __device__ void route_input(const SortArgs& a, long long start, long long n, boo
   *siOut = si; *tbOut = tb; *ntOut = nt;
 }
 
-// ---------------------------------------------------------------------------
-// COUNT phase: one warp chunk (kWarpChunk elements of a tile)
-// ---------------------------------------------------------------------------
-
 // Class counts from the six predicate totals #(k<p1), #(k<=p1), #(k<p2),
 // #(k<=p2), #(k<p3), #(k<=p3) of nt elements: class boundaries b1..b6 (max()
 // keeps them ordered when pivots are equal, which sends every key equal to a
 // pivot to the first equal pivot's class, as the reference's test order
-// does).  The map is additive over disjoint element sets, so per-chunk counts
-// sum to per-tile counts.
+// does).  The map is additive over disjoint element sets.
 __device__ __forceinline__ void classes_from_predicates(const int* pc, int nt, int* cnt) {
   int b[8];
   b[0] = 0;
@@ -277,35 +286,114 @@ __device__ __forceinline__ void classes_from_predicates(const int* pc, int nt, i
   for (int c = 0; c < 7; ++c) cnt[c] = b[c + 1] - b[c];
 }
 
-// Tile t, counted by one warp: the tile's keys against the segment's pivots,
-// chunk by chunk (the next chunk loads while the current one is counted); the
-// tile's class counts go to tileCnt.  Warps stream independently.
+// Class counts of one tile from its row of predicate totals (L2 reads).
+__device__ __forceinline__ void tile_classes(const int* row, int* cnt) {
+  const int4 r0 = __ldcg(reinterpret_cast<const int4*>(row));
+  const int4 r1 = __ldcg(reinterpret_cast<const int4*>(row) + 1);
+  const int pc[6] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y};
+  classes_from_predicates(pc, r1.z, cnt);
+}
+
+// ---------------------------------------------------------------------------
+// chunk pipeline (COUNT and SCATTER)
+// ---------------------------------------------------------------------------
+
+// A chunk can be bulk-copied when it lies inside the array and both source
+// addresses are 16-byte aligned (tiles start on absolute multiples of the
+// tile size, so this holds whenever the buffers are 16-byte aligned; the
+// check keeps any other case on plain loads).
 template <typename U, bool kIdx>
-__device__ __forceinline__ void count_tile_warp(const SortArgs& a, int level, int t) {
+__device__ __forceinline__ bool chunk_bulk_ok(const U* srcK, const int* srcI, long long c0,
+                                              long long n) {
+  constexpr int kWCH = Persist<U, kIdx>::kWCH;
+  if (c0 + kWCH > n) return false;
+  const unsigned long long ak = (unsigned long long)(srcK + c0);
+  const unsigned long long ai = kIdx ? (unsigned long long)(srcI + c0) : 0ull;
+  return ((ak | ai) & 15ull) == 0;
+}
+
+// Lane 0: bulk-copy the chunk at c0 (keys, and ids when withIds) into buffer b.
+template <typename U, bool kIdx, bool withIds>
+__device__ __forceinline__ void chunk_bulk_issue(typename Persist<U, kIdx>::WarpArea& ws, int b,
+                                                 const U* srcK, const int* srcI, long long c0) {
+  constexpr int kWCH = Persist<U, kIdx>::kWCH;
+  constexpr bool kI = kIdx && withIds;
+  constexpr unsigned kBytes = kWCH * sizeof(U) + (kI ? kWCH * 4 : 0);
+  fence_proxy_async();
+  mbar_arm(&ws.mbar[b], kBytes);
+  bulk_g2s(ws.pk[b], srcK + c0, kWCH * sizeof(U), &ws.mbar[b]);
+  if (kI) bulk_g2s(ws.pi[b], srcI + c0, kWCH * 4, &ws.mbar[b]);
+}
+
+// The lane's kItems consecutive keys of buffer b (flipped to unsigned images).
+template <typename U, bool kIdx>
+__device__ __forceinline__ void chunk_keys(const typename Persist<U, kIdx>::WarpArea& ws, int b,
+                                           int lane, typename Persist<U, kIdx>::KT flip,
+                                           typename Persist<U, kIdx>::KT* key) {
+  using KT = typename Persist<U, kIdx>::KT;
+  constexpr int kItems = Persist<U, kIdx>::kItems;
+  constexpr int kBytes = kItems * (int)sizeof(U);
+  using V = typename std::conditional<kBytes % 16 == 0, uint4, uint2>::type;
+  V v[kBytes / (int)sizeof(V)];
+  const V* pk = reinterpret_cast<const V*>(ws.pk[b] + lane * kItems);
+#pragma unroll
+  for (int j = 0; j < kBytes / (int)sizeof(V); ++j) v[j] = pk[j];
+  const U* u = reinterpret_cast<const U*>(v);
+#pragma unroll
+  for (int i = 0; i < kItems; ++i) key[i] = KT(u[i]) ^ flip;
+}
+
+// Bounded wait for buffer b's bulk copies; phases holds one parity bit per buffer.
+template <typename U, bool kIdx>
+__device__ __forceinline__ void chunk_wait(typename Persist<U, kIdx>::WarpArea& ws, int b,
+                                           unsigned& phases, Control* c) {
+  if (!mbar_wait(&ws.mbar[b], (phases >> b) & 1u)) set_error(c, kDevTimeout);
+  phases ^= 1u << b;
+}
+
+// ---------------------------------------------------------------------------
+// COUNT phase: one tile per warp
+// ---------------------------------------------------------------------------
+
+// Tile t, counted by one warp against its segment's pivots, chunk by chunk
+// (the next chunk is bulk-copied into the other buffer while the current one
+// is counted); lanes 0..6 store the tile's predicate totals and key count.
+template <typename U, bool kIdx>
+__device__ __forceinline__ void count_tile_warp(const SortArgs& a, int level, int t,
+                                                typename Persist<U, kIdx>::WarpArea& ws,
+                                                unsigned& phases) {
   using P = Persist<U, kIdx>;
   using KT = typename P::KT;
-  constexpr int kItems = P::kItems, kTile = P::kTile, kWCH = Geom<U>::kWarpChunk;
+  constexpr int kItems = P::kItems, kWCH = P::kWCH, kShift = P::kTileShift;
   const int par = level & 1;
   const int lane = threadIdx.x & 31;
   const U* src = (const U*)(par ? a.keysB : a.keysA);
   const KT flip = (KT)a.flip;
   const TileDesc td = load_tile(&a.tiles[par][t]);
-  const long long abs0 = (td.lo / kTile) * (long long)kTile;
+  const long long abs0 = (td.lo >> kShift) << kShift;
   const int rlo = (int)(td.lo - abs0), rhi = (int)(td.hi - abs0);
-  const U* tb = src + abs0;
-  const int chBeg = rlo / kWCH, chEnd = (rhi + kWCH - 1) / kWCH;
-  KT key[kItems];
-  unsigned okm = load_chunk<U, KT, kItems>(tb, abs0, a.n, chBeg * kWCH + lane * kItems, rlo, rhi,
-                                           flip, key);
   KT piv[3];
-  segment_pivots<KT, U>(a.segs[par][td.seg], src, level, flip, piv);
+  segment_pivots<KT, U>(&a.segs[par][td.seg], src, level, flip, piv);
+  const int chBeg = rlo / kWCH, chEnd = (rhi + kWCH - 1) / kWCH;
+  if (lane == 0 && chunk_bulk_ok<U, false>(src, nullptr, abs0 + (long long)chBeg * kWCH, a.n))
+    chunk_bulk_issue<U, kIdx, false>(ws, 0, src, nullptr, abs0 + (long long)chBeg * kWCH);
   unsigned w0 = 0, w1 = 0, w2 = 0;  // (k<p | k<=p << 16) for p1, p2, p3
   for (int ch = chBeg; ch < chEnd; ++ch) {
-    KT keyn[kItems];
-    unsigned okn = 0;
-    if (ch + 1 < chEnd)
-      okn = load_chunk<U, KT, kItems>(tb, abs0, a.n, (ch + 1) * kWCH + lane * kItems, rlo, rhi,
-                                      flip, keyn);
+    const int b = (ch - chBeg) & 1;
+    const long long c0 = abs0 + (long long)ch * kWCH;
+    if (ch + 1 < chEnd && lane == 0 && chunk_bulk_ok<U, false>(src, nullptr, c0 + kWCH, a.n))
+      chunk_bulk_issue<U, kIdx, false>(ws, b ^ 1, src, nullptr, c0 + kWCH);
+    const int e0 = ch * kWCH + lane * kItems;
+    KT key[kItems];
+    unsigned okm = 0;
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) okm |= (e0 + i >= rlo && e0 + i < rhi) ? (1u << i) : 0u;
+    if (chunk_bulk_ok<U, false>(src, nullptr, c0, a.n)) {
+      chunk_wait<U, kIdx>(ws, b, phases, a.ctrl);
+      chunk_keys<U, kIdx>(ws, b, lane, flip, key);
+    } else {
+      load_chunk<U, KT, kItems>(src + abs0, abs0, a.n, e0, rlo, rhi, flip, key);
+    }
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
       if (okm >> i & 1u) {
@@ -315,25 +403,16 @@ __device__ __forceinline__ void count_tile_warp(const SortArgs& a, int level, in
         w2 += (x < piv[2] ? 1u : 0u) + (x <= piv[2] ? 0x10000u : 0u);
       }
     }
-    okm = okn;
-#pragma unroll
-    for (int i = 0; i < kItems; ++i) key[i] = keyn[i];
+    __syncwarp();
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    w0 += __shfl_xor_sync(0xffffffffu, w0, o);
-    w1 += __shfl_xor_sync(0xffffffffu, w1, o);
-    w2 += __shfl_xor_sync(0xffffffffu, w2, o);
-  }
-  int pc[6], cc[7];
-  pc[0] = (int)(w0 & 0xffffu); pc[1] = (int)(w0 >> 16);
-  pc[2] = (int)(w1 & 0xffffu); pc[3] = (int)(w1 >> 16);
-  pc[4] = (int)(w2 & 0xffffu); pc[5] = (int)(w2 >> 16);
-  classes_from_predicates(pc, rhi - rlo, cc);
+  w0 = __reduce_add_sync(kFull, w0);
+  w1 = __reduce_add_sync(kFull, w1);
+  w2 = __reduce_add_sync(kFull, w2);
   if (lane < 8) {
-    int v = 0;
-#pragma unroll
-    for (int c = 0; c < 7; ++c) v = (lane == c) ? cc[c] : v;
+    const unsigned w = lane < 2 ? w0 : lane < 4 ? w1 : w2;
+    int v = (lane & 1) ? (int)(w >> 16) : (int)(w & 0xffffu);
+    if (lane == 6) v = rhi - rlo;
+    if (lane == 7) v = 0;
     a.tileCnt[par][(long long)t * 8 + lane] = v;
   }
 }
@@ -342,10 +421,11 @@ __device__ __forceinline__ void count_tile_warp(const SortArgs& a, int level, in
 // PLAN phase: one segment per CTA
 // ---------------------------------------------------------------------------
 
-// Turns the per-tile class counts of segment `seg` into destination offsets
-// (class bases as in turtle-sort.cu:755-761, then tiles in memory order, which
-// makes the partition stable), routes the children (turtle-sort.cu:857-933)
-// and stores the segment's sorted pivots and class table for SCATTER.
+// Turns the per-tile predicate totals of segment `seg` into class totals and
+// destination offsets (class bases as in turtle-sort.cu:755-761, then tiles
+// in memory order, which makes the partition stable), routes the children
+// (turtle-sort.cu:857-933) and stores the segment's sorted pivots, class
+// table and children for SCATTER.
 template <typename U, bool kIdx>
 __device__ __noinline__ void plan_segment(const SortArgs& a, int level, int seg,
                                           typename Persist<U, kIdx>::Smem& sm) {
@@ -355,8 +435,10 @@ __device__ __noinline__ void plan_segment(const SortArgs& a, int level, int seg,
   const int par = level & 1;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   SegDesc* sdp = &a.segs[par][seg];
-  if (tid == 0)
-    segment_pivots<KT, U>(*sdp, (const U*)(par ? a.keysB : a.keysA), level, (KT)a.flip, sm.piv);
+  if (tid == 0) {
+    segment_pivots<KT, U>(sdp, (const U*)(par ? a.keysB : a.keysA), level, (KT)a.flip, sm.piv);
+    sm.lut = pivot_lut(sm.piv[0] == sm.piv[1], sm.piv[1] == sm.piv[2]);
+  }
   const long long sdStart = __ldcg(&sdp->start);
   const int tileBase = __ldcg(&sdp->tileBase);
   const int nt = __ldcg(&sdp->ntiles);
@@ -366,32 +448,23 @@ __device__ __noinline__ void plan_segment(const SortArgs& a, int level, int seg,
   // thread `tid` owns the consecutive tiles [tid*per, (tid+1)*per)
   const int per = (nt + kThreads - 1) / kThreads;
   const int tBeg = min(nt, tid * per), tEnd = min(nt, tBeg + per);
-  long long s[7];
+  int s[7];
 #pragma unroll
   for (int c = 0; c < 7; ++c) s[c] = 0;
-  const int4* cnt4 = reinterpret_cast<const int4*>(cnt);
-  for (int t0 = tBeg; t0 < tEnd; t0 += 4) {
-    int4 r[8];
+  for (int t = tBeg; t < tEnd; ++t) {
+    int v[7];
+    tile_classes(cnt + (long long)t * 8, v);
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const bool ok = t0 + u < tEnd;
-      r[2 * u] = ok ? __ldcg(&cnt4[(long long)(t0 + u) * 2]) : make_int4(0, 0, 0, 0);
-      r[2 * u + 1] = ok ? __ldcg(&cnt4[(long long)(t0 + u) * 2 + 1]) : make_int4(0, 0, 0, 0);
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      s[0] += r[2 * u].x; s[1] += r[2 * u].y; s[2] += r[2 * u].z; s[3] += r[2 * u].w;
-      s[4] += r[2 * u + 1].x; s[5] += r[2 * u + 1].y; s[6] += r[2 * u + 1].z;
-    }
+    for (int c = 0; c < 7; ++c) s[c] += v[c];
   }
   // block exclusive scan of the per-thread sums, and the class totals
-  long long inc[7];
+  int inc[7];
 #pragma unroll
   for (int c = 0; c < 7; ++c) {
-    long long x = s[c];
+    int x = s[c];
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const long long y = __shfl_up_sync(0xffffffffu, x, o);
+      const int y = __shfl_up_sync(kFull, x, o);
       if (lane >= o) x += y;
     }
     inc[c] = x;
@@ -402,9 +475,9 @@ __device__ __noinline__ void plan_segment(const SortArgs& a, int level, int seg,
   }
   __syncthreads();
   if (tid < 7) {
-    long long acc = 0;
+    int acc = 0;
     for (int w = 0; w < kWarps; ++w) {
-      const long long x = sm.red[w][tid];
+      const int x = sm.red[w][tid];
       sm.red[w][tid] = acc;
       acc += x;
     }
@@ -412,37 +485,26 @@ __device__ __noinline__ void plan_segment(const SortArgs& a, int level, int seg,
   }
   __syncthreads();
   if (tid == 0) {
-    long long b = sdStart;
+    int b = 0;
     for (int c = 0; c < 7; ++c) { sm.cbase[c] = b; b += sm.tot[c]; }
     sm.cbase[7] = b;
   }
   __syncthreads();
+  // destination offsets of every tile
   {
-    long long run[7];
+    int run[7];
 #pragma unroll
     for (int c = 0; c < 7; ++c) run[c] = sm.cbase[c] + sm.red[warp][c] + (inc[c] - s[c]);
-    for (int t0 = tBeg; t0 < tEnd; t0 += 4) {
-      int4 r[8];
+    for (int t = tBeg; t < tEnd; ++t) {
+      int v[7];
+      tile_classes(cnt + (long long)t * 8, v);
+      longlong2* o = reinterpret_cast<longlong2*>(off + (long long)t * 8);
+      o[0] = make_longlong2(sdStart + run[0], sdStart + run[1]);
+      o[1] = make_longlong2(sdStart + run[2], sdStart + run[3]);
+      o[2] = make_longlong2(sdStart + run[4], sdStart + run[5]);
+      o[3] = make_longlong2(sdStart + run[6], 0);
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const bool ok = t0 + u < tEnd;
-        r[2 * u] = ok ? __ldcg(&cnt4[(long long)(t0 + u) * 2]) : make_int4(0, 0, 0, 0);
-        r[2 * u + 1] = ok ? __ldcg(&cnt4[(long long)(t0 + u) * 2 + 1]) : make_int4(0, 0, 0, 0);
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        if (t0 + u < tEnd) {
-          const int v[7] = {r[2 * u].x, r[2 * u].y, r[2 * u].z, r[2 * u].w,
-                            r[2 * u + 1].x, r[2 * u + 1].y, r[2 * u + 1].z};
-          longlong2* o = reinterpret_cast<longlong2*>(off + (long long)(t0 + u) * 8);
-          o[0] = make_longlong2(run[0], run[1]);
-          o[1] = make_longlong2(run[2], run[3]);
-          o[2] = make_longlong2(run[4], run[5]);
-          o[3] = make_longlong2(run[6], 0);
-#pragma unroll
-          for (int c = 0; c < 7; ++c) run[c] += v[c];
-        }
-      }
+      for (int c = 0; c < 7; ++c) run[c] += v[c];
     }
   }
 
@@ -451,8 +513,8 @@ __device__ __noinline__ void plan_segment(const SortArgs& a, int level, int seg,
   const int nextPar = par ^ 1;
   if (tid == 0) {
     for (int c = 0; c < 7; ++c) {
-      const long long pos = sm.cbase[c];
-      const long long m = sm.cbase[c + 1] - pos;
+      const long long pos = sdStart + sm.cbase[c];
+      const long long m = sm.cbase[c + 1] - sm.cbase[c];
       if (c & 1) {
         if (m > 0 && !dstIsA) push_fill(a, pos, m, (unsigned long long)sm.piv[c >> 1]);
         continue;
@@ -472,10 +534,10 @@ __device__ __noinline__ void plan_segment(const SortArgs& a, int level, int seg,
       sm.childStart[ci] = pos;
       sm.childN[ci] = m;
     }
-    for (int c = 0; c < 8; ++c) sdp->cbase[c] = sm.cbase[c];
-    for (int ci = 0; ci < 4; ++ci) sdp->childSeg[ci] = sm.childSeg[ci];
     for (int k = 0; k < 3; ++k) sdp->pivS[k] = (unsigned long long)sm.piv[k];
-    sdp->lut = pivot_lut(sm.piv[0] == sm.piv[1], sm.piv[1] == sm.piv[2]);
+    sdp->lut = sm.lut;
+    for (int c = 0; c < 8; ++c) sdp->cbase[c] = sdStart + sm.cbase[c];
+    for (int ci = 0; ci < 4; ++ci) sdp->childSeg[ci] = sm.childSeg[ci];
   }
   __syncthreads();
   for (int ci = 0; ci < 4; ++ci) {
@@ -489,192 +551,184 @@ __device__ __noinline__ void plan_segment(const SortArgs& a, int level, int seg,
 // ---------------------------------------------------------------------------
 // SCATTER phase: one tile per warp
 // ---------------------------------------------------------------------------
-// The warp walks its tile chunk by chunk (kWarpChunk elements; the next chunk
-// loads while the current one is written).  Per chunk it ranks the keys stably
-// per class (lane-local counts + a warp scan) and writes every element straight
-// to base[class] + rank, where base[class] starts at the tile's offset from the
-// plan and advances by each chunk's class counts.  Class runs of one chunk are
-// contiguous, and consecutive chunks continue each other's runs.
+
+// The warp walks its tile chunk by chunk (the next chunk is bulk-copied into
+// the other buffer while the current one is processed).  Per chunk: class of
+// every key (comparison sum through the segment's class table), lane-local
+// ranks in 4-bit counters, one warp scan of the packed counters, the chunk
+// staged by class, and each class run written to base[class] + rank, where
+// base[class] starts at the tile's offset from the plan and advances by each
+// chunk's class counts: class runs of one chunk are contiguous and
+// consecutive chunks continue them.  Lanes 0..11 watch the children's pivot
+// positions a[start+n/2], a[start], a[stop] (lane 3*child + j) and copy the
+// staged key that lands there into the child's descriptor.
 template <typename U, bool kIdx>
 __device__ __forceinline__ void scatter_tile_warp(const SortArgs& a, int level, int t,
-                                                  typename Persist<U, kIdx>::Smem& sm) {
+                                                  typename Persist<U, kIdx>::WarpArea& ws,
+                                                  unsigned& phases) {
   using P = Persist<U, kIdx>;
   using KT = typename P::KT;
-  constexpr int kItems = P::kItems, kTile = P::kTile, kWCH = Geom<U>::kWarpChunk;
+  constexpr int kItems = P::kItems, kWCH = P::kWCH, kShift = P::kTileShift;
   const int par = level & 1;
-  const bool dstIsA = (par == 1);
   const KT flip = (KT)a.flip;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
   const TileDesc td = load_tile(&a.tiles[par][t]);
-  const long long abs0 = (td.lo / kTile) * (long long)kTile;
+  const long long abs0 = (td.lo >> kShift) << kShift;
   const int rlo = (int)(td.lo - abs0), rhi = (int)(td.hi - abs0);
-  const U* tb = (const U*)(par ? a.keysB : a.keysA) + abs0;
-  const int* tbI = (par ? a.idxB : a.idxA) + abs0;
+  const U* srcK = (const U*)(par ? a.keysB : a.keysA);
+  const int* srcI = par ? a.idxB : a.idxA;
   const int chBeg = rlo / kWCH, chEnd = (rhi + kWCH - 1) / kWCH;
-  KT key[kItems];
-  int id[kIdx ? kItems : 1];
-  unsigned okm = load_chunk<U, KT, kItems>(tb, abs0, a.n, chBeg * kWCH + lane * kItems, rlo, rhi,
-                                           flip, key);
-  if (kIdx) load_ids<kItems>(tbI, abs0, a.n, chBeg * kWCH + lane * kItems, okm, id);
-  // segment metadata written by the plan (L2 reads: the plan ran on another SM)
+  if (lane == 0 && chunk_bulk_ok<U, kIdx>(srcK, srcI, abs0 + (long long)chBeg * kWCH, a.n))
+    chunk_bulk_issue<U, kIdx, true>(ws, 0, srcK, srcI, abs0 + (long long)chBeg * kWCH);
   const SegDesc* sdp = &a.segs[par][td.seg];
   const KT p1 = (KT)__ldcg(&sdp->pivS[0]), p2 = (KT)__ldcg(&sdp->pivS[1]),
            p3 = (KT)__ldcg(&sdp->pivS[2]);
   const unsigned lut = __ldcg(&sdp->lut);
-  // lanes 0..6: running destination base of class `lane`; lanes 0..11: the
-  // children's pivot candidate positions a[start+n/2], a[start], a[stop]
-  long long base = lane < 7 ? __ldcg(&a.tileOff[par][(long long)t * 8 + lane]) : 0;
-  long long cpos = -1;
-  int cchild = -1;
+  // running destination of each class; pivot positions of the children
+  if (lane < 7) ws.wbase[lane] = __ldcg(&a.tileOff[par][(long long)t * 8 + lane]);
+  bool watch = false;
   if (lane < 12) {
-    const int ci = lane / 3, j = lane - 3 * ci, c = 2 * ci;
-    cchild = __ldcg(&sdp->childSeg[ci]);
-    if (cchild >= 0) {
-      const long long cb = __ldcg(&sdp->cbase[c]), cn = __ldcg(&sdp->cbase[c + 1]) - cb;
+    const int ci = lane / 3, j = lane - 3 * (lane / 3);
+    const int child = __ldcg(&sdp->childSeg[ci]);
+    long long cpos = -1;
+    if (child >= 0) {
+      const long long cb = __ldcg(&sdp->cbase[2 * ci]);
+      const long long cn = __ldcg(&sdp->cbase[2 * ci + 1]) - cb;
       cpos = j == 0 ? cb + cn / 2 : j == 1 ? cb : cb + cn - 1;
     }
+    ws.cpos[lane] = cpos;
+    ws.cseg[lane] = child;
+    watch = child >= 0;
   }
-  U* dst = (U*)(par ? a.keysA : a.keysB);
-  int* dstI = par ? a.idxA : a.idxB;
-  long long* wb = sm.wbase[warp];
-  constexpr int kStride = kWCH + kWCH / 32;  // padded stage slice per warp
-  static_assert(kWarps * kStride <= Geom<U>::kKeySlots, "stage slices exceed the key stage");
-  static_assert(!kIdx || kWarps * kStride <= Geom<U>::kIdxSlots, "stage slices exceed the id stage");
-  KT* skeys = sm.keys + warp * kStride;
-  int* sidx = sm.idx + (kIdx ? warp * kStride : 0);
-  unsigned* sdst = sm.dstRel + warp * kStride;
-  const long long segStartOf = __ldcg(&sdp->start);
+  watch = __any_sync(kFull, watch);
+  __syncwarp();
+
   for (int ch = chBeg; ch < chEnd; ++ch) {
-    KT keyn[kItems];
-    int idn[kIdx ? kItems : 1];
-    unsigned okn = 0;
-    if (ch + 1 < chEnd) {
-      const int en = (ch + 1) * kWCH + lane * kItems;
-      okn = load_chunk<U, KT, kItems>(tb, abs0, a.n, en, rlo, rhi, flip, keyn);
-      if (kIdx) load_ids<kItems>(tbI, abs0, a.n, en, okn, idn);
-    }
-    // classes and lane-local ranks (memory order inside the lane's items)
-    unsigned long long acc = 0;       // 8-bit count per class
-    unsigned info[(kItems + 3) / 4];  // (class | local rank << 3) per element
+    const int b = (ch - chBeg) & 1;
+    const long long c0 = abs0 + (long long)ch * kWCH;
+    if (ch + 1 < chEnd && lane == 0 && chunk_bulk_ok<U, kIdx>(srcK, srcI, c0 + kWCH, a.n))
+      chunk_bulk_issue<U, kIdx, true>(ws, b ^ 1, srcK, srcI, c0 + kWCH);
+    const int e0 = ch * kWCH + lane * kItems;  // tile-relative index of the lane's first key
+    KT key[kItems];
+    unsigned okm = 0;
 #pragma unroll
-    for (int j = 0; j < (kItems + 3) / 4; ++j) info[j] = 0;
+    for (int i = 0; i < kItems; ++i) okm |= (e0 + i >= rlo && e0 + i < rhi) ? (1u << i) : 0u;
+    if (chunk_bulk_ok<U, kIdx>(srcK, srcI, c0, a.n)) {
+      chunk_wait<U, kIdx>(ws, b, phases, a.ctrl);
+      chunk_keys<U, kIdx>(ws, b, lane, flip, key);
+    } else {
+      // array end: plain loads; the ids go through the buffer like bulk ones
+      load_chunk<U, KT, kItems>(srcK + abs0, abs0, a.n, e0, rlo, rhi, flip, key);
+      if (kIdx) {
+        int id[kItems];
+        load_ids<kItems>(srcI + abs0, abs0, a.n, e0, okm, id);
+#pragma unroll
+        for (int i = 0; i < kItems; ++i) ws.pi[b][lane * kItems + i] = id[i];
+      }
+    }
+
+    // classes (3 bits each, 7 = no key) and lane-local ranks (4 bits each)
+    unsigned cw = 0, rw = 0, acc = 0;
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
-      unsigned code = 0xffu;
+      unsigned c = 7u;
       if (okm >> i & 1u) {
-        const int c = class_lut<KT>(key[i], p1, p2, p3, lut);
-        const unsigned lr = (unsigned)(acc >> (8 * c)) & 0xffu;
-        acc += 1ull << (8 * c);
-        code = (unsigned)c | (lr << 3);
+        const KT k = key[i];
+        const unsigned cp = (unsigned)((k > p1) + (k >= p1) + (k > p2) + (k >= p2) + (k > p3) +
+                                       (k >= p3));
+        c = (lut >> (3u * cp)) & 7u;
+        rw |= ((acc >> (4u * c)) & 15u) << (4 * i);
+        acc += 1u << (4u * c);
       }
-      info[i >> 2] |= code << (8 * (i & 3));
+      cw |= c << (3 * i);
     }
-    // warp exclusive scan of the lane counts (four words of 16-bit fields)
-    unsigned w[4], ex[4], tot[4];
-    w[0] = (unsigned)(acc & 0xff) | (unsigned)((acc >> 8) & 0xff) << 16;
-    w[1] = (unsigned)((acc >> 16) & 0xff) | (unsigned)((acc >> 24) & 0xff) << 16;
-    w[2] = (unsigned)((acc >> 32) & 0xff) | (unsigned)((acc >> 40) & 0xff) << 16;
-    w[3] = (unsigned)((acc >> 48) & 0xff);
+    // warp exclusive scan of the lane counts (8-bit fields; exclusive sums
+    // stay below 256, so the packed arithmetic is exact)
+    const unsigned a0 = (acc & 0xFu) | ((acc & 0xF0u) << 4) | ((acc & 0xF00u) << 8) |
+                        ((acc & 0xF000u) << 12);
+    const unsigned a1 = ((acc >> 16) & 0xFu) | ((acc >> 12) & 0xF00u) | ((acc >> 8) & 0xF0000u);
+    unsigned i0 = a0, i1 = a1;
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      unsigned x = w[q];
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-      }
-      ex[q] = x - w[q];
-      tot[q] = __shfl_sync(0xffffffffu, x, 31);
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y0 = __shfl_up_sync(kFull, i0, o), y1 = __shfl_up_sync(kFull, i1, o);
+      if (lane >= o) { i0 += y0; i1 += y1; }
     }
-    if (lane < 7) wb[lane] = base;
-    __syncwarp();
-    // stage the chunk class by class in the warp's slice, with each element's
-    // destination relative to the segment start (bit 31: a pivot-run key that
-    // waits in B for its fill)
-    int cs[8];
+    // class totals of the chunk (16-bit fields) and class starts in the stage
+    const unsigned t01 = __reduce_add_sync(kFull, (acc & 0xFu) | ((acc & 0xF0u) << 12));
+    const unsigned t23 = __reduce_add_sync(kFull, ((acc >> 8) & 0xFu) | ((acc & 0xF000u) << 4));
+    const unsigned t45 = __reduce_add_sync(kFull, ((acc >> 16) & 0xFu) | ((acc >> 4) & 0xF0000u));
+    const unsigned t6 = __reduce_add_sync(kFull, (acc >> 24) & 0xFu);
+    const unsigned cs1 = t01 & 0xFFFFu;
+    const unsigned cs2 = cs1 + (t01 >> 16);
+    const unsigned cs3 = cs2 + (t23 & 0xFFFFu);
+    const unsigned cs4 = cs3 + (t23 >> 16);
+    const unsigned cs5 = cs4 + (t45 & 0xFFFFu);
+    const unsigned cs6 = cs5 + (t45 >> 16);
+    const unsigned nv = cs6 + t6;
+    // stage the chunk: per lane and class, the slot of the lane's first key of
+    // that class is a packed 8-bit field of b0 (classes 0-3) or b1 (4-6)
     {
-      int run = 0;
+      const unsigned b0 = (cs1 << 8) + (cs2 << 16) + (cs3 << 24) + (i0 - a0);
+      const unsigned b1 = cs4 + (cs5 << 8) + (cs6 << 16) + (i1 - a1);
 #pragma unroll
-      for (int c = 0; c < 7; ++c) {
-        cs[c] = run;
-        run += (int)((tot[c >> 1] >> (16 * (c & 1))) & 0xffffu);
-      }
-      cs[7] = run;
-    }
-    const long long segStart = segStartOf;
+      for (int h = 0; h < kItems; h += 4) {
+        int4 idv = make_int4(0, 0, 0, 0);
+        if (kIdx) idv = *reinterpret_cast<const int4*>(&ws.pi[b][lane * kItems + h]);
+        const int idq[4] = {idv.x, idv.y, idv.z, idv.w};
 #pragma unroll
-    for (int i = 0; i < kItems; ++i) {
-      const unsigned code = (info[i >> 2] >> (8 * (i & 3))) & 0xffu;
-      if (code != 0xffu) {
-        const int c = code & 7;
-        const int q = c >> 1;
-        const unsigned eq = q == 0 ? ex[0] : q == 1 ? ex[1] : q == 2 ? ex[2] : ex[3];
-        const unsigned rk = ((eq >> (16 * (c & 1))) & 0xffffu) + (code >> 3);
-        const int pos = cs[c] + (int)rk;
-        const int sp = pos + (pos >> 5);
-        skeys[sp] = key[i];
-        if (kIdx) sidx[sp] = id[i];
-        const unsigned rel = (unsigned)(wb[c] - segStart) + rk;
-        sdst[sp] = ((c & 1) && !dstIsA) ? (rel | 0x80000000u) : rel;
-      }
-    }
-    __syncwarp();
-    // write out: consecutive stage slots of one class go to consecutive addresses
-    {
-      const int n = cs[7];
-#pragma unroll
-      for (int j = 0; j < kItems; ++j) {
-        const int i = lane + 32 * j;
-        if (i < n) {
-          const int sp = i + (i >> 5);
-          const unsigned rel = sdst[sp];
-          const long long d = segStart + (long long)(rel & 0x7fffffffu);
-          if (!(rel & 0x80000000u)) dst[d] = U(skeys[sp] ^ flip);
-          if (kIdx) dstI[d] = sidx[sp];
-        }
-      }
-    }
-    // a child pivot candidate written by this chunk: the lane holding it
-    // records the key (rare; one ballot otherwise)
-    {
-      bool in = false;
-      long long r = 0;
-      if (lane < 12 && cchild >= 0) {
-        const int c = 2 * (lane / 3);
-        const unsigned cnt = (tot[c >> 1] >> (16 * (c & 1))) & 0xffffu;
-        r = cpos - wb[c];
-        in = r >= 0 && r < (long long)cnt;
-      }
-      unsigned m = __ballot_sync(0xffffffffu, in);
-      while (m) {
-        const int srcl = __ffs(m) - 1;
-        m &= m - 1;
-        const int c = 2 * (srcl / 3), j = srcl - 3 * (srcl / 3);
-        const int rr = (int)__shfl_sync(0xffffffffu, r, srcl);
-        const int child = __shfl_sync(0xffffffffu, cchild, srcl);
-        const unsigned eq = (ex[c >> 1] >> (16 * (c & 1))) & 0xffffu;
-        const unsigned cn = (w[c >> 1] >> (16 * (c & 1))) & 0xffffu;
-        if ((unsigned)rr >= eq && (unsigned)rr < eq + cn) {  // exactly one lane
-          const unsigned want = (unsigned)rr - eq;
-#pragma unroll
-          for (int i = 0; i < kItems; ++i) {
-            const unsigned code = (info[i >> 2] >> (8 * (i & 3))) & 0xffu;
-            if (code != 0xffu && (int)(code & 7) == c && (code >> 3) == want)
-              a.segs[par ^ 1][child].piv[j] = (unsigned long long)key[i];
+        for (int u = 0; u < 4; ++u) {
+          const int i = h + u;
+          const unsigned c = (cw >> (3 * i)) & 7u;
+          if (c != 7u) {
+            const unsigned w = c < 4u ? b0 : b1;
+            const unsigned pos = ((w >> ((c & 3u) * 8u)) & 0xFFu) + ((rw >> (4 * i)) & 15u);
+            ws.sk[pos] = key[i];
+            if (kIdx) ws.si[pos] = idq[u];
+            ws.sc[pos] = (unsigned char)c;
           }
         }
       }
     }
-    __syncwarp();
-    // advance the running bases by this chunk's class counts
-    if (lane < 7) base += (long long)((tot[lane >> 1] >> (16 * (lane & 1))) & 0xffffu);
-    okm = okn;
-#pragma unroll
-    for (int i = 0; i < kItems; ++i) key[i] = keyn[i];
-    if (kIdx) {
-#pragma unroll
-      for (int i = 0; i < kItems; ++i) id[i] = idn[i];
+    // lanes 0..6: destination table of the chunk, then advance the bases
+    if (lane < 7) {
+      const unsigned csl = lane == 1 ? cs1 : lane == 2 ? cs2 : lane == 3 ? cs3 : lane == 4 ? cs4
+                         : lane == 5 ? cs5 : lane == 6 ? cs6 : 0u;
+      const unsigned cel = lane == 0 ? cs1 : lane == 1 ? cs2 : lane == 2 ? cs3 : lane == 3 ? cs4
+                         : lane == 4 ? cs5 : lane == 5 ? cs6 : nv;
+      const long long wb = ws.wbase[lane];
+      ws.delta[lane] = wb - (long long)csl;
+      ws.wbase[lane] = wb + (long long)(cel - csl);
     }
+    __syncwarp();
+    // write-out: consecutive stage slots of one class go to consecutive addresses
+    {
+      U* dstK = (U*)(par ? a.keysA : a.keysB);
+      int* dstI = par ? a.idxA : a.idxB;
+      const bool parkPivots = (par == 0);  // children in B: pivot-run keys wait for their fill
+#pragma unroll
+      for (int j = 0; j < kItems; ++j) {
+        const int sl = 32 * j + lane;
+        if (sl < (int)nv) {
+          const unsigned c = ws.sc[sl];
+          const long long d = ws.delta[c] + sl;
+          if (!(parkPivots && (c & 1u))) dstK[d] = U(ws.sk[sl] ^ flip);
+          if (kIdx) dstI[d] = ws.si[sl];
+        }
+      }
+    }
+    // a child's pivot position written by this chunk: copy its key
+    if (watch && lane < 12) {
+      const int child = ws.cseg[lane];
+      if (child >= 0) {
+        const int ci = lane / 3;
+        const unsigned csA = ci == 0 ? 0u : ci == 1 ? cs2 : ci == 2 ? cs4 : cs6;
+        const unsigned csB = ci == 0 ? cs1 : ci == 1 ? cs3 : ci == 2 ? cs5 : nv;
+        const long long r = ws.cpos[lane] - ws.delta[2 * ci];
+        if (r >= (long long)csA && r < (long long)csB)
+          a.segs[par ^ 1][child].piv[lane - 3 * ci] = (unsigned long long)ws.sk[r];
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -743,17 +797,19 @@ __device__ __noinline__ bool leaf_bucket(const SortArgs& a, typename Persist<U, 
 // next tile before the warp works on the current one).
 template <typename U, bool kIdx, int kPhase>
 __device__ __forceinline__ void stream_tiles(const SortArgs& a, int level, int ntiles,
-                                             unsigned* wc, typename Persist<U, kIdx>::Smem& sm) {
+                                             unsigned* wc,
+                                             typename Persist<U, kIdx>::WarpArea& ws,
+                                             unsigned& mphase) {
   const int lane = threadIdx.x & 31;
   unsigned t = 0;
   if (lane == 0) t = atomicAdd(wc, 1u);
-  t = __shfl_sync(0xffffffffu, t, 0);
+  t = __shfl_sync(kFull, t, 0);
   while ((int)t < ntiles) {
     unsigned nxt = 0;
     if (lane == 0) nxt = atomicAdd(wc, 1u);
-    if (kPhase == 0) count_tile_warp<U, kIdx>(a, level, (int)t);
-    else scatter_tile_warp<U, kIdx>(a, level, (int)t, sm);
-    t = __shfl_sync(0xffffffffu, nxt, 0);
+    if (kPhase == 0) count_tile_warp<U, kIdx>(a, level, (int)t, ws, mphase);
+    else scatter_tile_warp<U, kIdx>(a, level, (int)t, ws, mphase);
+    t = __shfl_sync(kFull, nxt, 0);
   }
 }
 
@@ -765,6 +821,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
   typename P::Smem& sm = *reinterpret_cast<typename P::Smem*>(smem_raw);
   Control* c = a.ctrl;
   const int tid = threadIdx.x;
+  typename P::WarpArea& ws = sm.w[tid >> 5];
+  unsigned mphase = 0;  // parity bit of each chunk buffer's barrier
+  if ((tid & 31) == 0) { mbar_init(&ws.mbar[0], 1); mbar_init(&ws.mbar[1], 1); }
+  __syncwarp();
   int phase = 0;
   int level = 0;
   timeline_mark(c, -1);
@@ -829,9 +889,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
       break;
     }
 
-    // COUNT: per-tile class counts
+    // COUNT: per-tile predicate totals
     if (blockIdx.x == 0 && tid == 0) c->work[(phase + 2) & 3] = 0;
-    stream_tiles<U, kIdx, 0>(a, level, ntiles, &c->work[phase & 3], sm);
+    stream_tiles<U, kIdx, 0>(a, level, ntiles, &c->work[phase & 3], ws, mphase);
     ++phase;
     __threadfence();
     if (!grid_barrier(c)) return;
@@ -859,7 +919,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
       st.store(0ull, cuda::memory_order_relaxed);
       c->work[(phase + 2) & 3] = 0;
     }
-    stream_tiles<U, kIdx, 1>(a, level, ntiles, &c->work[phase & 3], sm);
+    stream_tiles<U, kIdx, 1>(a, level, ntiles, &c->work[phase & 3], ws, mphase);
     ++phase;
     __threadfence();
     if (!grid_barrier(c)) return;
