@@ -236,6 +236,7 @@ def run_gpu(args) -> None:
         dist.barrier()
     torch.cuda.synchronize()
     launches0 = sorter.launches
+    sorter.time_kernels(True)
     clocks = ClockSampler(Path(args.clocks_csv) if args.clocks_csv else None)
     events = []
     with clocks:
@@ -246,6 +247,10 @@ def run_gpu(args) -> None:
         t_wall = time.perf_counter() - t_wall0
     sorter.status(sh)
     launches = sorter.launches - launches0
+    nk, part_ms, leaf_ms = sorter.kernel_times(args.steps)
+    sorter.time_kernels(False)
+    part_ms /= max(nk, 1)
+    leaf_ms /= max(nk, 1)
     ms = [a.elapsed_time(b) for a, b in events]
     tot_ms = sum(ms)
     if dist is not None:
@@ -281,8 +286,12 @@ def run_gpu(args) -> None:
     if rank != 0:
         return
     peak, peak_kind = peaks()
+    # two-pass bound of the sort: read + write keys and ids twice; each of the
+    # two kernels (partition, leaf) is charged one of the passes
     alg_bytes = 4.0 * n * (4 + 4)
-    achieved = alg_bytes / (ms_step / 1e3) / 1e9
+    part_bytes = alg_bytes / 2
+    achieved = part_bytes / (part_ms / 1e3) / 1e9
+    sort_achieved = alg_bytes / (ms_step / 1e3) / 1e9
     traffic = profile_traffic(n)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -296,8 +305,12 @@ def run_gpu(args) -> None:
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": f"{peak_kind} hbm_gbs",
-                     "algorithmic_bytes": alg_bytes,
-                     "kernel": "persistent_sort_kernel<uint32_t,true> (one launch per sort)"},
+                     "kernel": "persistent_sort_kernel<uint32_t,true> (one launch per sort)",
+                     "algorithmic_bytes_per_launch": part_bytes,
+                     "algorithmic_bytes_note": "one read + one write of keys and ids (2*n*8 B), "
+                                               "half of the sort's two-pass bound 4*n*8 B",
+                     "kernel_ms": part_ms, "leaf_kernel_ms": leaf_ms,
+                     "sort_achieved": sort_achieved, "sort_frac": sort_achieved / peak},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 8,
                 "d2h_bytes_per_step": n * 8,
                 "path": "turtle_start/turtle_sync (StartSorting/Sync) with pinned host buffers"},
@@ -323,9 +336,22 @@ def main() -> None:
     ap.add_argument("--n", type=int, default=1 << 26)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--clocks-csv", default=None)
+    ap.add_argument("--workload", default="sort64m",
+                    choices=["sort64m", "plain12m", "sweep", "multisort", "batched", "wide",
+                             "serving"],
+                    help="sort64m (default) is the headline line; the others print their own")
+    ap.add_argument("--requests", type=int, default=1000, help="serving: requests in the sample")
+    ap.add_argument("--rate", type=float, default=0.0,
+                    help="serving: arrivals per second (0: 1.5x the serial StartSorting rate)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
+    if args.impl == "gb300" and args.workload != "sort64m":
+        import torch
+        import bench_workloads
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        bench_workloads.WORKLOADS[args.workload](args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -1,0 +1,388 @@
+"""The non-default benchmark workloads of bench.py (one JSON line each).
+
+    python bench.py --workload plain12m   # 12,582,912 int32, index = value
+    python bench.py --workload sweep      # 2^26 int32+idx, distributions a-e
+    python bench.py --workload multisort  # 262,144 arrays x 1024 int32
+    python bench.py --workload batched    # 100,000 uneven arrays, int32 and int16
+    python bench.py --workload wide       # int64 2^28 + idx, uint8 2^30, uint16 2^29 Zipf
+    python bench.py --workload serving    # Poisson request stream through the server
+
+Every device-resident time is taken with CUDA events on the sorter's launch
+stream; every end-to-end time includes the host<->device copies of pinned
+host buffers.  Each result is checked (sorted, permutation of the input)
+outside the timed region.
+"""
+from __future__ import annotations
+
+import json
+import threading
+import time
+
+import numpy as np
+
+import turtlesort_gb300 as ts
+from turtlesort_gb300 import datagen as dg
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _pinned(torch, arr: np.ndarray):
+    """A pinned host copy of arr (torch tensor kept alive by the caller) and its numpy view."""
+    t = torch.empty(arr.nbytes, dtype=torch.uint8, pin_memory=True)
+    v = t.numpy().view(arr.dtype)[: arr.size]
+    v[:] = arr
+    return t, v
+
+
+def _check(keys_in: np.ndarray, out: np.ndarray, ids_in: np.ndarray | None,
+           ids_out: np.ndarray | None) -> None:
+    """Sorted output; with ids, ids_out is the stable reordering of ids_in
+    (checked through the keys when ids are positions, else as the values)."""
+    if out.size > 1 and not np.all(out[:-1] <= out[1:]):
+        raise RuntimeError("output not sorted")
+    if ids_out is None:
+        return
+    if ids_in is not None and ids_in.size and ids_in[-1] == ids_in.size - 1 and ids_in[0] == 0:
+        if not np.array_equal(keys_in[ids_out], out):
+            raise RuntimeError("ids are not the sorting permutation")
+    elif not np.array_equal(ids_out, out.astype(np.int32)):
+        raise RuntimeError("ids initialised to the values no longer equal them")
+
+
+def _device_sort_times(torch, sorter, keys: np.ndarray, idx: np.ndarray | None, steps: int,
+                       warmup: int):
+    """ms per device-resident sort (restore copy untimed), partition/leaf split."""
+    dev = torch.device("cuda", torch.cuda.current_device())
+    tk = torch.from_numpy(keys.view(np.uint8).copy()).to(dev)
+    k = torch.empty_like(tk)
+    ti = torch.from_numpy(idx).to(dev) if idx is not None else None
+    i = torch.empty_like(ti) if ti is not None else None
+    stream = torch.cuda.Stream(device=dev)
+    sh = stream.cuda_stream
+    ev = []
+    for s in range(warmup + steps):
+        if s == warmup:
+            sorter.time_kernels(True)
+        with torch.cuda.stream(stream):
+            k.copy_(tk)
+            if i is not None:
+                i.copy_(ti)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            sorter.sort_device(k.data_ptr(), i.data_ptr() if i is not None else None, keys.size, sh)
+            e1.record(stream)
+        if s >= warmup:
+            ev.append((e0, e1))
+    sorter.status(sh)
+    ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+    nk, pm, lm = sorter.kernel_times(steps)
+    sorter.time_kernels(False)
+    out = k.cpu().numpy().view(keys.dtype)
+    out_i = i.cpu().numpy() if i is not None else None
+    _check(keys, out, idx, out_i)
+    return ms, (pm / max(nk, 1)), (lm / max(nk, 1))
+
+
+def _e2e_sort_times(sorter, keys: np.ndarray, idx: np.ndarray | None, steps: int, warmup: int):
+    torch = _torch()
+    hk_t, hk = _pinned(torch, keys)
+    hi_t, hi = (_pinned(torch, idx) if idx is not None else (None, None))
+    secs = []
+    for s in range(warmup + steps):
+        hk[:] = keys
+        if hi is not None:
+            hi[:] = idx
+        sorter.StartSorting(hk, hi)
+        t = sorter.Sync()
+        if s >= warmup:
+            secs.append(t)
+    _check(keys, hk, idx, hi)
+    return sum(secs) / len(secs)
+
+
+def _line(metric, value, unit, args, cfg, extra):
+    d = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
+         "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+         "vs_baseline": None, "data": "synthetic (splitmix64, seeds 0x7475727431 + workload)",
+         "config": cfg}
+    d.update(extra)
+    print(json.dumps(d), flush=True)
+
+
+def _sort_line(args, name, keys, idx, dtype_name, note=""):
+    torch = _torch()
+    n = keys.size
+    width = keys.dtype.itemsize
+    with ts.TurtleSort(keys.dtype, n, track_index=idx is not None) as s:
+        ms, pm, lm = _device_sort_times(torch, s, keys, idx, args.steps, args.warmup)
+        e2e = _e2e_sort_times(s, keys, idx, args.steps, args.warmup)
+        levels = s.last_levels
+    per = width + (4 if idx is not None else 0)
+    alg = 4.0 * n * per
+    _line(f"sorted keys/s ({name}, device-resident)", n / (ms / 1e3), "keys/s", args,
+          {"workload": name, "n": n, "key": dtype_name, "payload": "int32" if idx is not None else "none",
+           "note": note},
+          {"dtype": dtype_name, "ms_per_step": ms,
+           "roofline_sort": {"algorithmic_bytes": alg, "achieved_gbs": alg / (ms / 1e3) / 1e9},
+           "kernel_ms": {"partition": pm, "leaf": lm},
+           "e2e": {"value": n / e2e, "unit": "keys/s", "h2d_bytes_per_step": n * per,
+                   "d2h_bytes_per_step": n * per},
+           "levels": levels})
+
+
+def plain12m(args):
+    keys, idx = dg.plain_sort_input()
+    _sort_line(args, "12,582,912 int32 in [0,2^31-1], index = value", keys, idx, "int32",
+               "the reference README benchmark shape; ids start as the values")
+
+
+def sweep(args):
+    for kind, desc in [("a", "uniform"), ("b", "uniform [0,1023]"), ("c", "sorted"),
+                       ("d", "reverse sorted"), ("e", "sorted + n/20 random swaps")]:
+        keys, idx = dg.sweep_input(kind, 1 << 26)
+        _sort_line(args, f"2^26 int32+idx, {desc}", keys, idx, "int32")
+
+
+def wide(args):
+    keys = dg.uniform(np.int64, 1 << 28, dg.seed_for(3))
+    idx = np.arange(keys.size, dtype=np.int32)
+    _sort_line(args, "2^28 int64 full range + int32 index", keys, idx, "int64")
+    del keys, idx
+    keys = dg.uniform(np.uint8, 1 << 30, dg.seed_for(3) + 1)
+    _sort_line(args, "2^30 uint8 in [0,255], keys only", keys, None, "u8")
+    del keys
+    keys = dg.zipf_u16(1 << 29, dg.seed_for(3) + 2)
+    _sort_line(args, "2^29 uint16 Zipf(1.1) over 65536 ranks, keys only", keys, None, "u16")
+
+
+def multisort(args):
+    torch = _torch()
+    num, arr = 262_144, 1024
+    keys = dg.uniform(np.int32, num * arr, dg.seed_for(2) + 7)
+    with ts.TurtleSort(np.int32, num * arr, track_index=False) as s:
+        # device-resident
+        dev = torch.device("cuda", torch.cuda.current_device())
+        tk = torch.from_numpy(keys).to(dev)
+        k = torch.empty_like(tk)
+        stream = torch.cuda.Stream(device=dev)
+        ev = []
+        for st in range(args.warmup + args.steps):
+            with torch.cuda.stream(stream):
+                k.copy_(tk)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                s.multisort_device(k.data_ptr(), None, arr, num, stream.cuda_stream)
+                e1.record(stream)
+            if st >= args.warmup:
+                ev.append((e0, e1))
+        s.status(stream.cuda_stream)
+        ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+        out = k.cpu().numpy().reshape(num, arr)
+        if not np.array_equal(out, np.sort(keys.reshape(num, arr), axis=1)):
+            raise RuntimeError("multisort result differs")
+        # end to end through MultiSort (host pointer, copies included)
+        hk_t, hk = _pinned(torch, keys)
+        secs = []
+        for st in range(args.warmup + args.steps):
+            hk[:] = keys
+            t = s.MultiSort(arr, num, hk, block_size=32)
+            if st >= args.warmup:
+                secs.append(t)
+        e2e = sum(secs) / len(secs)
+    _line("sorted arrays/s (262,144 x 1024 int32 MultiSort, device-resident)", num / (ms / 1e3),
+          "arrays/s", args, {"workload": "262,144 arrays x 1024 int32 uniform", "arrays": num,
+                             "arr_size": arr},
+          {"dtype": "int32", "ms_per_step": ms, "keys_per_s": num * arr / (ms / 1e3),
+           "e2e": {"value": num / e2e, "unit": "arrays/s", "h2d_bytes_per_step": num * arr * 4,
+                   "d2h_bytes_per_step": num * arr * 4}})
+
+
+def batched(args):
+    torch = _torch()
+    for dtype, name in [(np.int32, "int32"), (np.int16, "int16")]:
+        keys, offs, _ = dg.batched_input(dtype)
+        num, total = offs.size - 1, int(offs[-1])
+        with ts.TurtleSort(dtype, total, track_index=False) as s:
+            dev = torch.device("cuda", torch.cuda.current_device())
+            tk = torch.from_numpy(keys.view(np.uint8).copy()).to(dev)
+            k = torch.empty_like(tk)
+            to = torch.from_numpy(offs).to(dev)
+            stream = torch.cuda.Stream(device=dev)
+            ev = []
+            for st in range(args.warmup + args.steps):
+                with torch.cuda.stream(stream):
+                    k.copy_(tk)
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    s.sort_batched_device(k.data_ptr(), None, to.data_ptr(), num, total,
+                                          stream.cuda_stream)
+                    e1.record(stream)
+                if st >= args.warmup:
+                    ev.append((e0, e1))
+            s.status(stream.cuda_stream)
+            ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+            out = k.cpu().numpy().view(dtype)
+            for a in range(0, num, max(1, num // 500)):  # spot check 500 arrays
+                lo, hi = int(offs[a]), int(offs[a + 1])
+                if not np.array_equal(out[lo:hi], np.sort(keys[lo:hi])):
+                    raise RuntimeError(f"batched array {a} differs")
+            # end to end: pinned host keys -> device -> one batched sort -> host
+            hk_t, hk = _pinned(torch, keys)
+            secs = []
+            for st in range(args.warmup + args.steps):
+                hk[:] = keys
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                with torch.cuda.stream(stream):
+                    k.view(torch.uint8).copy_(hk_t[: keys.nbytes], non_blocking=True)
+                    s.sort_batched_device(k.data_ptr(), None, to.data_ptr(), num, total,
+                                          stream.cuda_stream)
+                    hk_t[: keys.nbytes].copy_(k.view(torch.uint8), non_blocking=True)
+                stream.synchronize()
+                s.status(stream.cuda_stream)
+                if st >= args.warmup:
+                    secs.append(time.perf_counter() - t0)
+            e2e = sum(secs) / len(secs)
+        # the reference-style baseline: one StartSorting + Sync per array
+        sample = 3000
+        with ts.TurtleSort(dtype, int(np.max(np.diff(offs))), track_index=False) as s1:
+            hk_t, hk = _pinned(torch, keys[: int(offs[sample])])
+            t0 = time.perf_counter()
+            for a in range(sample):
+                lo, hi = int(offs[a]), int(offs[a + 1])
+                s1.StartSorting(hk[lo:hi])
+                s1.Sync()
+            per_array = (time.perf_counter() - t0) / sample
+        _line(f"sorted arrays/s (100,000 uneven {name} arrays, one batched launch, end to end)",
+              num / e2e, "arrays/s", args,
+              {"workload": f"100,000 {name} arrays, lengths floor(exp(U(ln 16, ln 65536))), "
+                           f"{total} keys, offsets array", "arrays": num, "keys": total},
+              {"dtype": name, "ms_per_step_device": ms, "device_arrays_per_s": num / (ms / 1e3),
+               "device_keys_per_s": total / (ms / 1e3),
+               "e2e": {"value": num / e2e, "unit": "arrays/s",
+                       "h2d_bytes_per_step": keys.nbytes, "d2h_bytes_per_step": keys.nbytes},
+               "per_array_startsorting_arrays_per_s": 1.0 / per_array,
+               "per_array_sample": f"first {sample} arrays, StartSorting+Sync each, pinned",
+               "speedup_vs_per_array": (num / e2e) * per_array})
+
+
+def serving(args):
+    """A bounded sample of the serving stream: args.requests requests with
+    Poisson arrivals, log-uniform sizes in [1024, 16 * 2^20], dtype int32 60% /
+    int64 25% / uint16 15%, half with ids, HBM budget 64 GB."""
+    torch = _torch()
+    nreq = args.requests
+    rng_u = dg.uniform_real(4 * nreq, dg.seed_for(4))
+    sizes = np.floor(np.exp(np.log(1024) + rng_u[:nreq] * (np.log(16 << 20) - np.log(1024)))).astype(np.int64)
+    dts = np.where(rng_u[nreq:2 * nreq] < 0.60, 0, np.where(rng_u[nreq:2 * nreq] < 0.85, 1, 2))
+    with_idx = rng_u[2 * nreq:3 * nreq] < 0.5
+    dtypes = [np.int32, np.int64, np.uint16]
+    pool = dg.uniform(np.uint64, 1 << 25, dg.seed_for(4) + 1)  # 256 MiB of random words
+    maxb = int(sizes.max()) * 8
+    nslots = 12
+    slot_k = [torch.empty(maxb, dtype=torch.uint8, pin_memory=True) for _ in range(nslots)]
+    slot_i = [torch.empty(int(sizes.max()) * 4, dtype=torch.uint8, pin_memory=True)
+              for _ in range(nslots)]
+
+    def fill(r, slot):
+        dt = np.dtype(dtypes[dts[r]])
+        n = int(sizes[r])
+        words = (n * dt.itemsize + 7) // 8
+        off = int((r * 7919) % (pool.size - words))
+        kv = slot_k[slot].numpy()[: n * dt.itemsize].view(dt)
+        kv[:] = pool[off: off + words].view(dt)[:n]
+        iv = None
+        if with_idx[r]:
+            iv = slot_i[slot].numpy()[: n * 4].view(np.int32)
+            iv[:] = np.arange(n, dtype=np.int32)
+        return kv, iv
+
+    # serial baseline: one StartSorting + Sync per request, back to back
+    sorters = {}
+    t_serial = 0.0
+    keys_total = int(sizes.sum())
+    for r in range(nreq):
+        kv, iv = fill(r, 0)
+        key = (dts[r], bool(with_idx[r]))
+        if key not in sorters:
+            sorters[key] = ts.TurtleSort(dtypes[dts[r]], int(sizes.max()), track_index=key[1])
+        t0 = time.perf_counter()
+        sorters[key].StartSorting(kv, iv)
+        sorters[key].Sync()
+        t_serial += time.perf_counter() - t0
+    for s in sorters.values():
+        s.close()
+    serial_kps = keys_total / t_serial
+    # Poisson arrivals offering 1.5x the serial rate
+    rate = args.rate if args.rate > 0 else 1.5 * nreq / t_serial
+    gaps = -np.log(np.maximum(rng_u[3 * nreq:4 * nreq], 1e-12)) / rate
+    arrivals = np.cumsum(gaps)
+    free = list(range(nslots))
+    cv = threading.Condition()
+    lat = []
+    pending = []
+    srv = ts.TurtleServer(hbm_budget_bytes=64 << 30)
+
+    def waiter():
+        while True:
+            with cv:
+                while not pending:
+                    cv.wait()
+                item = pending.pop(0)
+            if item is None:
+                return
+            r, ticket, slot, kv, t_arr = item
+            srv.wait(ticket)
+            done = time.perf_counter()
+            if kv.size > 1 and not np.all(kv[:-1] <= kv[1:]):
+                raise RuntimeError(f"request {r} not sorted")
+            with cv:
+                lat.append(done - t_arr)
+                free.append(slot)
+                cv.notify_all()
+
+    th = threading.Thread(target=waiter)
+    th.start()
+    t_start = time.perf_counter()
+    for r in range(nreq):
+        target = t_start + arrivals[r]
+        now = time.perf_counter()
+        if target > now:
+            time.sleep(target - now)
+        with cv:
+            while not free:
+                cv.wait()
+            slot = free.pop()
+        kv, iv = fill(r, slot)
+        ticket = srv.submit(kv, iv)
+        with cv:
+            pending.append((r, ticket, slot, kv, max(target, t_start)))
+            cv.notify_all()
+    with cv:
+        pending.append(None)
+        cv.notify_all()
+    th.join()
+    t_total = time.perf_counter() - t_start
+    st = srv.stats()
+    srv.close()
+    lat_ms = np.array(lat) * 1e3
+    _line("served keys/s (Poisson request stream, continuous batching)", keys_total / t_total,
+          "keys/s", args,
+          {"workload": f"{nreq} requests (bounded sample of 20,000), sizes log-uniform "
+                       f"[1024, 16*2^20], int32 60%/int64 25%/uint16 15%, half with ids, "
+                       f"HBM budget 64 GB", "requests": nreq, "keys": keys_total,
+           "arrival_rate_per_s": rate},
+          {"dtype": "mixed", "p50_ms": float(np.percentile(lat_ms, 50)),
+           "p99_ms": float(np.percentile(lat_ms, 99)),
+           "server_p50_ms": st["p50_ms"], "server_p99_ms": st["p99_ms"],
+           "batches": st["batches"], "serial_startsorting_keys_per_s": serial_kps,
+           "speedup_vs_serial": (keys_total / t_total) / serial_kps,
+           "e2e": {"value": keys_total / t_total, "unit": "keys/s",
+                   "note": "host buffers pinned; copies inside every request's latency"}})
+
+
+WORKLOADS = {"plain12m": plain12m, "sweep": sweep, "wide": wide, "multisort": multisort,
+             "batched": batched, "serving": serving}

@@ -231,6 +231,17 @@ void turtle_debug_fail_allocations(int count);
  * entries written (at most max). */
 int turtle_debug_timeline(const turtle_sorter* s, uint64_t* ns, int32_t* info, int max);
 
+/* Kernel timing for measurement: with enable != 0, every later sort on this
+ * sorter records CUDA events on its launch stream before the partition
+ * kernel, between it and the leaf kernel, and after the leaf kernel (graph-
+ * captured batched sorts excepted).  Resets the count of timed sorts. */
+turtle_status turtle_debug_time_kernels(turtle_sorter* s, int enable);
+
+/* Sums over the last `last` timed sorts (at most 64) of the partition
+ * kernel's and the leaf kernel's durations in milliseconds; waits for those
+ * sorts.  Returns the number of sorts summed (0 if timing is off). */
+int turtle_debug_kernel_times(turtle_sorter* s, int last, double* partition_ms, double* leaf_ms);
+
 /* Library version string (static storage). */
 const char* turtle_version(void);
 

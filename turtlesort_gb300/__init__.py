@@ -203,6 +203,17 @@ class TurtleSort:
     def last_levels(self) -> int:
         return int(self._lib.turtle_last_levels(self._h))
 
+    def time_kernels(self, enable: bool = True) -> None:
+        """Record CUDA events around the partition and leaf kernels of every
+        later sort (see kernel_times)."""
+        _check(self._lib.turtle_debug_time_kernels(self._h, int(enable)), "time_kernels", self._h)
+
+    def kernel_times(self, last: int):
+        """(sorts, partition_ms, leaf_ms) summed over the last `last` timed sorts."""
+        pm, lm = C.c_double(), C.c_double()
+        n = self._lib.turtle_debug_kernel_times(self._h, int(last), C.byref(pm), C.byref(lm))
+        return int(n), float(pm.value), float(lm.value)
+
 
 class TurtleServer:
     """Continuous-batching sort server over the C ABI (turtle_server_*).

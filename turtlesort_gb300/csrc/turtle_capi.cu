@@ -66,6 +66,11 @@ struct turtle_sorter {
   bool lastHasIdx = false;
   bool lastValid = false;
   cudaStream_t lastStream = nullptr;
+  // optional kernel timing: events around the two launches of each sort
+  static constexpr int kRing = 64;
+  bool timeKernels = false;
+  cudaEvent_t ev[kRing][3] = {};
+  long long timed = 0;
 };
 
 namespace {
@@ -107,13 +112,22 @@ turtle::SortArgs make_args(turtle_sorter* s, void* keys, int32_t* idx, const lon
 // Enqueue: reset the control block, run the persistent kernel, copy the
 // control block to the pinned status block.
 cudaError_t enqueue_persistent(turtle_sorter* s, const turtle::SortArgs& a, bool hasIdx,
-                               cudaStream_t st) {
+                               cudaStream_t st, bool allowTiming = true) {
   if (!a.resume) {
     cudaError_t e = cudaMemsetAsync(a.ctrl, 0, sizeof(turtle::Control), st);
     if (e != cudaSuccess) return e;
   }
-  cudaError_t e = turtle::kernels_launch_persistent(s->width, hasIdx, a, s->grid[hasIdx ? 1 : 0], st);
+  const bool timing = allowTiming && s->timeKernels;
+  cudaEvent_t* ev = s->ev[s->timed % turtle_sorter::kRing];
+  cudaError_t e = cudaSuccess;
+  if (timing && (e = cudaEventRecord(ev[0], st)) != cudaSuccess) return e;
+  e = turtle::kernels_launch_persistent(s->width, hasIdx, a, s->grid[hasIdx ? 1 : 0], st,
+                                        timing ? ev[1] : nullptr);
   if (e != cudaSuccess) return e;
+  if (timing) {
+    if ((e = cudaEventRecord(ev[2], st)) != cudaSuccess) return e;
+    ++s->timed;
+  }
   s->launches.fetch_add(2);  // partition + leaf kernel
   s->lastArgs = a;
   s->lastArgs.resume = 1;
@@ -234,6 +248,10 @@ turtle_status turtle_destroy(turtle_sorter* s) {
   if (!s) return TURTLE_OK;
   cudaSetDevice(s->device);
   if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->lastStream) cudaStreamSynchronize(s->lastStream);
+  for (auto& r : s->ev)
+    for (auto& e : r)
+      if (e) { cudaEventDestroy(e); e = nullptr; }
   free_graphs(s);
   turtle::vmm_free(&s->keysA);
   turtle::vmm_free(&s->keysB);
@@ -413,7 +431,7 @@ turtle_status turtle_sort_batched_device(turtle_sorter* s, void* d_keys, int32_t
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   TRY_CUDA(s, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-  cudaError_t ce = enqueue_persistent(s, a, hasIdx, s->stream);
+  cudaError_t ce = enqueue_persistent(s, a, hasIdx, s->stream, false);
   s->launches.fetch_sub(2);  // counted when the graph is launched
   cudaError_t ee = cudaStreamEndCapture(s->stream, &graph);
   if (ce != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return from_cuda(s, ce); }
@@ -488,6 +506,38 @@ int turtle_debug_timeline(const turtle_sorter* s, uint64_t* ns, int32_t* info, i
   ns[n] = s->hctrl->tEnd;
   info[n] = -2;
   return n + 1;
+}
+
+turtle_status turtle_debug_time_kernels(turtle_sorter* s, int enable) {
+  if (!s) return TURTLE_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(s->device);
+  if (enable && !s->ev[0][0]) {
+    for (auto& r : s->ev)
+      for (auto& e : r) TRY_CUDA(s, cudaEventCreate(&e));
+  }
+  s->timeKernels = enable != 0;
+  s->timed = 0;
+  return TURTLE_OK;
+}
+
+int turtle_debug_kernel_times(turtle_sorter* s, int last, double* partition_ms, double* leaf_ms) {
+  if (!s || !s->timeKernels || last <= 0) return 0;
+  const long long n = std::min<long long>(std::min<long long>(last, s->timed), turtle_sorter::kRing);
+  double pm = 0, lm = 0;
+  for (long long k = s->timed - n; k < s->timed; ++k) {
+    cudaEvent_t* ev = s->ev[k % turtle_sorter::kRing];
+    float a = 0, b = 0;
+    if (cudaEventSynchronize(ev[2]) != cudaSuccess || cudaEventElapsedTime(&a, ev[0], ev[1]) != cudaSuccess ||
+        cudaEventElapsedTime(&b, ev[1], ev[2]) != cudaSuccess) {
+      cudaGetLastError();
+      return 0;
+    }
+    pm += a;
+    lm += b;
+  }
+  if (partition_ms) *partition_ms = pm;
+  if (leaf_ms) *leaf_ms = lm;
+  return (int)n;
 }
 
 const char* turtle_version(void) { return "turtle-gb300 0.1 (sm_103a)"; }

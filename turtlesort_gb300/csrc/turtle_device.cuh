@@ -28,7 +28,10 @@ namespace turtle {
 constexpr int kThreads = TURTLE_PART_THREADS;  // CTA size of the partition kernel
 constexpr int kWarps = kThreads / 32;
 constexpr int kMinBlocks = TURTLE_PART_BLOCKS; // resident partition CTAs per SM we compile for
-constexpr int kPartTile = 4096;          // partition tile (keys), a power of two
+#ifndef TURTLE_PART_TILE
+#define TURTLE_PART_TILE 4096
+#endif
+constexpr int kPartTile = TURTLE_PART_TILE;  // partition tile (keys), a power of two
 constexpr int kLThreads = 512;           // CTA size of the leaf / batched kernels
 constexpr int kLWarps = kLThreads / 32;
 constexpr int kFillChunk = 1 << 16;      // pivot-run fill work unit (elements)
@@ -92,6 +95,9 @@ struct SegDesc {        // a segment partitioned by the multi-CTA 3-pivot pass
   int pad;
   long long cbase[8];   // class boundaries after planning (cbase[7] = end)
   int childSeg[4];      // next-level segment of classes 0,2,4,6 (-1: none)
+  int tot[8];           // class totals, summed by COUNT
+  int planBase;         // first plan item of this segment
+  int pad2;
 };
 struct TileDesc {       // one partition tile: [lo, hi) of segment seg
   long long lo;
@@ -113,6 +119,7 @@ struct FillDesc {       // a pivot run parked in scratch: keys filled by value
 
 struct Control {
   unsigned long long segTile[2];  // packed (segments << 32 | tiles) per level parity
+  int planCount[2];               // plan items per level parity
   int leafCount;
   int fillCount;
   int classCount[16];
@@ -152,10 +159,11 @@ struct SortArgs {
   int* tileCnt[2];           // [tile][8]: #(k<p1), #(k<=p1), #(k<p2), #(k<=p2), #(k<p3),
                              // #(k<=p3), #keys (predicate totals against the segment's pivots)
   long long* tileOff[2];     // [tile][8] global destination of each class
+  int* planSeg[2];           // segment of each plan item (kPartTile * kThreads keys)
   LeafDesc* leaves;
   LeafDesc* leavesSorted;
   FillDesc* fills;
-  int segCap, tileCap, leafCap, fillCap;
+  int segCap, tileCap, leafCap, fillCap, planCap;
   int resume;                // 1: continue a partition that yielded
   Control* ctrl;
 };
@@ -262,6 +270,10 @@ __device__ __forceinline__ void mbar_init(unsigned long long* m, unsigned count)
 // just read.
 __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async;\n" ::: "memory");
+}
+// The same for shared memory only (buffer reuse inside a warp).
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
 }
 __device__ __forceinline__ void mbar_arm(unsigned long long* m, unsigned bytes) {
   asm volatile(

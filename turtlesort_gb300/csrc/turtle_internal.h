@@ -12,8 +12,10 @@ struct SortArgs;
 // ---- kernels (turtle_sort.cu) ----
 // width = key bytes (1, 2, 4, 8); hasIdx = int32 payload present.
 cudaError_t kernels_prepare(int width, bool hasIdx, int device, int* grid);
+// Launches the partition kernel and the leaf kernel on `stream`; when `mid`
+// is not null it is recorded between the two launches.
 cudaError_t kernels_launch_persistent(int width, bool hasIdx, const SortArgs& a, int grid,
-                                      cudaStream_t stream);
+                                      cudaStream_t stream, cudaEvent_t mid = nullptr);
 cudaError_t kernels_launch_multisort(int width, bool hasIdx, void* keys, int* idx,
                                      long long numArrays, int arrSize, unsigned long long flip,
                                      cudaStream_t stream);

@@ -13,7 +13,8 @@ namespace turtle {
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 struct WsLayout {
-  int segCap = 0, tileCap = 0, leafCap = 0, fillCap = 0;
+  int segCap = 0, tileCap = 0, leafCap = 0, fillCap = 0, planCap = 0;
+  size_t offPlanSeg[2] = {0, 0};
   size_t offCtrl = 0, offSegs[2] = {0, 0}, offTiles[2] = {0, 0}, offTileCnt[2] = {0, 0},
          offTileOff[2] = {0, 0};
   size_t offLeaves = 0, offLeavesSorted = 0, offFills = 0, bytes = 0;
@@ -28,6 +29,9 @@ inline WsLayout make_layout(long long maxN, int tile, int leafMax, long long ext
   // ordinary inputs (one level adds at most 4 leaves and 3 fills per segment)
   const long long leafCap = std::max(8 * (segCap + 1), maxN / 64) + extraLeaves + 4096;
   const long long fillCap = 2 * (3 * (segCap + 1) + tileCap) + maxN / 64 + 4096;
+  // plan items: kThreads tiles each, at least one per segment
+  const long long planCap = tileCap / turtle::kThreads + segCap + 64;
+  L.planCap = (int)planCap;
   L.segCap = (int)segCap;
   L.tileCap = (int)tileCap;
   L.leafCap = (int)leafCap;
@@ -38,6 +42,7 @@ inline WsLayout make_layout(long long maxN, int tile, int leafMax, long long ext
   for (int p = 0; p < 2; ++p) { L.offTiles[p] = o; o = align_up(o + tileCap * sizeof(turtle::TileDesc), 256); }
   for (int p = 0; p < 2; ++p) { L.offTileCnt[p] = o; o = align_up(o + tileCap * 8 * sizeof(int), 256); }
   for (int p = 0; p < 2; ++p) { L.offTileOff[p] = o; o = align_up(o + tileCap * 8 * sizeof(long long), 256); }
+  for (int p = 0; p < 2; ++p) { L.offPlanSeg[p] = o; o = align_up(o + planCap * sizeof(int), 256); }
   L.offLeaves = o; o = align_up(o + leafCap * sizeof(turtle::LeafDesc), 256);
   L.offLeavesSorted = o; o = align_up(o + leafCap * sizeof(turtle::LeafDesc), 256);
   L.offFills = o; o = align_up(o + fillCap * sizeof(turtle::FillDesc), 256);
@@ -85,6 +90,7 @@ inline SortArgs bind_args(void* keys, int* idx, void* keysB, int* idxB, char* ws
     a.tiles[p] = (TileDesc*)(ws + L.offTiles[p]);
     a.tileCnt[p] = (int*)(ws + L.offTileCnt[p]);
     a.tileOff[p] = (long long*)(ws + L.offTileOff[p]);
+    a.planSeg[p] = (int*)(ws + L.offPlanSeg[p]);
   }
   a.leaves = (LeafDesc*)(ws + L.offLeaves);
   a.leavesSorted = (LeafDesc*)(ws + L.offLeavesSorted);
@@ -93,6 +99,7 @@ inline SortArgs bind_args(void* keys, int* idx, void* keysB, int* idxB, char* ws
   a.tileCap = L.tileCap;
   a.leafCap = L.leafCap;
   a.fillCap = L.fillCap;
+  a.planCap = L.planCap;
   a.ctrl = (Control*)(ws + L.offCtrl);
   return a;
 }

@@ -8,12 +8,13 @@
 // separated by a bounded grid barrier:
 //   COUNT   one warp per tile (kTile keys of one segment, aligned to absolute
 //           kTile boundaries) counts its keys against the segment's pivots
-//           (six predicate totals).
-//   PLAN    one CTA per segment turns the per-tile totals into class totals
-//           and per-tile destination offsets (class order as in
-//           turtle-sort.cu:755-761, then tiles in memory order: stable) and
-//           routes the children (next-level segments with their tiles,
-//           leaves, parked pivot runs; turtle-sort.cu:857-933).
+//           (six predicate totals per tile; class totals per segment).
+//   PLAN    one CTA per plan item (kThreads tiles of one segment) turns the
+//           per-tile totals into per-tile destination offsets (class order as
+//           in turtle-sort.cu:755-761, then tiles in memory order: stable);
+//           a segment's first item also routes its children (next-level
+//           segments with their tiles, leaves, parked pivot runs;
+//           turtle-sort.cu:857-933).
 //   SCATTER one warp per tile, 256-key chunks prefetched into shared memory
 //           by bulk asynchronous copies (TMA).  Per chunk the warp ranks the
 //           keys stably per class (4-bit per-lane counters, one warp scan),
@@ -87,6 +88,8 @@ struct Persist {
   struct Smem {  // partition CTA
     WarpArea w[kWarps];
     int red[kWarps][8];
+    int redPre[kWarps][8];
+    int pre[8];
     int tot[8];
     int cbase[8];                   // class boundaries relative to the segment start
     int childSeg[4];
@@ -178,7 +181,9 @@ __device__ int alloc_segment(const SortArgs& a, int par, long long start, long l
       atomicAdd(&a.ctrl->segTile[par], (1ull << 32) | (unsigned long long)nt);
   const int si = (int)(old >> 32);
   const long long tb = (long long)(old & 0xffffffffull);
-  if (si >= a.segCap || tb + nt > a.tileCap) {
+  const int np = (int)((nt + kThreads - 1) / kThreads);  // plan items
+  const int pb = atomicAdd(&a.ctrl->planCount[par], np);
+  if (si >= a.segCap || tb + nt > a.tileCap || pb + np > a.planCap) {
     set_error(a.ctrl, kDevCapacity);
     return -1;
   }
@@ -187,9 +192,11 @@ __device__ int alloc_segment(const SortArgs& a, int par, long long start, long l
   d.piv[0] = d.piv[1] = d.piv[2] = 0;
   d.pivS[0] = d.pivS[1] = d.pivS[2] = 0;
   d.lut = 0; d.pad = 0;
-  for (int c = 0; c < 8; ++c) d.cbase[c] = 0;
+  for (int c = 0; c < 8; ++c) { d.cbase[c] = 0; d.tot[c] = 0; }
   for (int c = 0; c < 4; ++c) d.childSeg[c] = -1;
+  d.planBase = pb; d.pad2 = 0;
   a.segs[par][si] = d;
+  for (int k = 0; k < np; ++k) a.planSeg[par][pb + k] = si;
   *tbOut = (int)tb;
   *ntOut = (int)nt;
   return si;
@@ -319,7 +326,7 @@ __device__ __forceinline__ void chunk_bulk_issue(typename Persist<U, kIdx>::Warp
   constexpr int kWCH = Persist<U, kIdx>::kWCH;
   constexpr bool kI = kIdx && withIds;
   constexpr unsigned kBytes = kWCH * sizeof(U) + (kI ? kWCH * 4 : 0);
-  fence_proxy_async();
+  fence_proxy_async_smem();
   mbar_arm(&ws.mbar[b], kBytes);
   bulk_g2s(ws.pk[b], srcK + c0, kWCH * sizeof(U), &ws.mbar[b]);
   if (kI) bulk_g2s(ws.pi[b], srcI + c0, kWCH * 4, &ws.mbar[b]);
@@ -361,7 +368,7 @@ __device__ __forceinline__ void chunk_wait(typename Persist<U, kIdx>::WarpArea& 
 template <typename U, bool kIdx>
 __device__ __forceinline__ void count_tile_warp(const SortArgs& a, int level, int t,
                                                 typename Persist<U, kIdx>::WarpArea& ws,
-                                                unsigned& phases) {
+                                                unsigned& phases, int& accSeg, int& accCnt) {
   using P = Persist<U, kIdx>;
   using KT = typename P::KT;
   constexpr int kItems = P::kItems, kWCH = P::kWCH, kShift = P::kTileShift;
@@ -415,100 +422,117 @@ __device__ __forceinline__ void count_tile_warp(const SortArgs& a, int level, in
     if (lane == 7) v = 0;
     a.tileCnt[par][(long long)t * 8 + lane] = v;
   }
+  // the tile's class counts go to the warp's running total of its segment
+  {
+    const int pc[6] = {(int)(w0 & 0xffffu), (int)(w0 >> 16), (int)(w1 & 0xffffu),
+                       (int)(w1 >> 16), (int)(w2 & 0xffffu), (int)(w2 >> 16)};
+    int cc[7];
+    classes_from_predicates(pc, rhi - rlo, cc);
+    int mine = 0;
+#pragma unroll
+    for (int c = 0; c < 7; ++c) mine = lane == c ? cc[c] : mine;
+    if (td.seg != accSeg) {
+      if (accSeg >= 0 && lane < 7 && accCnt) atomicAdd(&a.segs[par][accSeg].tot[lane], accCnt);
+      accSeg = td.seg;
+      accCnt = 0;
+    }
+    accCnt += mine;
+  }
 }
 
 // ---------------------------------------------------------------------------
-// PLAN phase: one segment per CTA
+// PLAN phase: one plan item per CTA
 // ---------------------------------------------------------------------------
 
-// Turns the per-tile predicate totals of segment `seg` into class totals and
-// destination offsets (class bases as in turtle-sort.cu:755-761, then tiles
-// in memory order, which makes the partition stable), routes the children
+// One plan item: kThreads consecutive tiles (item j of segment `seg`, one
+// tile per thread).  The class bases of the segment follow from its class
+// totals (summed by COUNT) in class order as in turtle-sort.cu:755-761; the
+// tiles before the item contribute their counts (summed by the whole CTA),
+// and the item's own tiles are scanned in memory order, which makes the
+// partition stable.  Item 0 of a segment also routes the children
 // (turtle-sort.cu:857-933) and stores the segment's sorted pivots, class
-// table and children for SCATTER.
+// table and children for SCATTER.  Large segments are thus planned by many
+// CTAs at once.
 template <typename U, bool kIdx>
-__device__ __noinline__ void plan_segment(const SortArgs& a, int level, int seg,
-                                          typename Persist<U, kIdx>::Smem& sm) {
+__device__ __noinline__ void plan_item(const SortArgs& a, int level, int item,
+                                       typename Persist<U, kIdx>::Smem& sm) {
   using P = Persist<U, kIdx>;
   using KT = typename P::KT;
   constexpr int kTile = P::kTile, kLeafMax = P::kLeafMax;
   const int par = level & 1;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int seg = __ldcg(&a.planSeg[par][item]);
   SegDesc* sdp = &a.segs[par][seg];
-  if (tid == 0) {
-    segment_pivots<KT, U>(sdp, (const U*)(par ? a.keysB : a.keysA), level, (KT)a.flip, sm.piv);
-    sm.lut = pivot_lut(sm.piv[0] == sm.piv[1], sm.piv[1] == sm.piv[2]);
-  }
+  const int j = item - __ldcg(&sdp->planBase);
   const long long sdStart = __ldcg(&sdp->start);
   const int tileBase = __ldcg(&sdp->tileBase);
   const int nt = __ldcg(&sdp->ntiles);
   const int* cnt = a.tileCnt[par] + (long long)tileBase * 8;
-  long long* off = a.tileOff[par] + (long long)tileBase * 8;
-
-  // thread `tid` owns the consecutive tiles [tid*per, (tid+1)*per)
-  const int per = (nt + kThreads - 1) / kThreads;
-  const int tBeg = min(nt, tid * per), tEnd = min(nt, tBeg + per);
-  int s[7];
-#pragma unroll
-  for (int c = 0; c < 7; ++c) s[c] = 0;
-  for (int t = tBeg; t < tEnd; ++t) {
-    int v[7];
-    tile_classes(cnt + (long long)t * 8, v);
-#pragma unroll
-    for (int c = 0; c < 7; ++c) s[c] += v[c];
+  const int t0 = j * kThreads;
+  if (tid < 7) sm.tot[tid] = __ldcg(&sdp->tot[tid]);
+  if (j == 0 && tid == 0) {
+    segment_pivots<KT, U>(sdp, (const U*)(par ? a.keysB : a.keysA), level, (KT)a.flip, sm.piv);
+    sm.lut = pivot_lut(sm.piv[0] == sm.piv[1], sm.piv[1] == sm.piv[2]);
   }
-  // block exclusive scan of the per-thread sums, and the class totals
+  // counts of the segment's tiles before this item, and of this thread's tile
+  int pre[7], v[7];
+#pragma unroll
+  for (int c = 0; c < 7; ++c) { pre[c] = 0; v[c] = 0; }
+  for (int t = tid; t < t0; t += kThreads) {
+    int w[7];
+    tile_classes(cnt + (long long)t * 8, w);
+#pragma unroll
+    for (int c = 0; c < 7; ++c) pre[c] += w[c];
+  }
+  const int myTile = t0 + tid;
+  if (myTile < nt) tile_classes(cnt + (long long)myTile * 8, v);
   int inc[7];
 #pragma unroll
   for (int c = 0; c < 7; ++c) {
-    int x = s[c];
+    const int ps = (int)__reduce_add_sync(kFull, (unsigned)pre[c]);
+    int x = v[c];
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const int y = __shfl_up_sync(kFull, x, o);
       if (lane >= o) x += y;
     }
     inc[c] = x;
-  }
-  if (lane == 31) {
-#pragma unroll
-    for (int c = 0; c < 7; ++c) sm.red[warp][c] = inc[c];
+    if (lane == 31) { sm.red[warp][c] = x; sm.redPre[warp][c] = ps; }
   }
   __syncthreads();
   if (tid < 7) {
-    int acc = 0;
+    int acc = 0, pacc = 0;
     for (int w = 0; w < kWarps; ++w) {
       const int x = sm.red[w][tid];
       sm.red[w][tid] = acc;
       acc += x;
+      pacc += sm.redPre[w][tid];
     }
-    sm.tot[tid] = acc;
+    sm.pre[tid] = pacc;
   }
-  __syncthreads();
   if (tid == 0) {
     int b = 0;
     for (int c = 0; c < 7; ++c) { sm.cbase[c] = b; b += sm.tot[c]; }
     sm.cbase[7] = b;
   }
   __syncthreads();
-  // destination offsets of every tile
-  {
-    int run[7];
+  if (myTile < nt) {
+    long long o[7];
 #pragma unroll
-    for (int c = 0; c < 7; ++c) run[c] = sm.cbase[c] + sm.red[warp][c] + (inc[c] - s[c]);
-    for (int t = tBeg; t < tEnd; ++t) {
-      int v[7];
-      tile_classes(cnt + (long long)t * 8, v);
-      longlong2* o = reinterpret_cast<longlong2*>(off + (long long)t * 8);
-      o[0] = make_longlong2(sdStart + run[0], sdStart + run[1]);
-      o[1] = make_longlong2(sdStart + run[2], sdStart + run[3]);
-      o[2] = make_longlong2(sdStart + run[4], sdStart + run[5]);
-      o[3] = make_longlong2(sdStart + run[6], 0);
-#pragma unroll
-      for (int c = 0; c < 7; ++c) run[c] += v[c];
-    }
+    for (int c = 0; c < 7; ++c)
+      o[c] = sdStart + sm.cbase[c] + sm.pre[c] + sm.red[warp][c] + (inc[c] - v[c]);
+    longlong2* dst = reinterpret_cast<longlong2*>(a.tileOff[par] + (long long)(tileBase + myTile) * 8);
+    dst[0] = make_longlong2(o[0], o[1]);
+    dst[1] = make_longlong2(o[2], o[3]);
+    dst[2] = make_longlong2(o[4], o[5]);
+    dst[3] = make_longlong2(o[6], 0);
+  }
+  if (j != 0) {
+    __syncthreads();
+    return;
   }
 
-  // children: thread 0 routes them; the CTA writes the tile descriptors
+  // item 0: children -- thread 0 routes them; the CTA writes the tile descriptors
   const bool dstIsA = (par == 1);
   const int nextPar = par ^ 1;
   if (tid == 0) {
@@ -801,16 +825,22 @@ __device__ __forceinline__ void stream_tiles(const SortArgs& a, int level, int n
                                              typename Persist<U, kIdx>::WarpArea& ws,
                                              unsigned& mphase) {
   const int lane = threadIdx.x & 31;
+  // the bulk copies of this phase read what other CTAs wrote before the
+  // grid barrier: order the async proxy after it
+  if (lane == 0) fence_proxy_async();
   unsigned t = 0;
   if (lane == 0) t = atomicAdd(wc, 1u);
   t = __shfl_sync(kFull, t, 0);
+  int accSeg = -1, accCnt = 0;
   while ((int)t < ntiles) {
     unsigned nxt = 0;
     if (lane == 0) nxt = atomicAdd(wc, 1u);
-    if (kPhase == 0) count_tile_warp<U, kIdx>(a, level, (int)t, ws, mphase);
+    if (kPhase == 0) count_tile_warp<U, kIdx>(a, level, (int)t, ws, mphase, accSeg, accCnt);
     else scatter_tile_warp<U, kIdx>(a, level, (int)t, ws, mphase);
     t = __shfl_sync(kFull, nxt, 0);
   }
+  if (kPhase == 0 && accSeg >= 0 && lane < 7 && accCnt)
+    atomicAdd(&a.segs[level & 1][accSeg].tot[lane], accCnt);
 }
 
 template <typename U, bool kIdx>
@@ -877,6 +907,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
     const unsigned long long v = st.load(cuda::memory_order_acquire);
     const int nsegs = (int)(v >> 32);
     const int ntiles = (int)(v & 0xffffffffull);
+    const int nplan = ld_acquire_int(&c->planCount[par]);
     if (nsegs == 0) break;
     if (level >= kMaxLevels) { if (tid == 0) set_error(c, kDevCapacity); return; }
     if (ld_acquire_int(&c->leafCount) > a.leafCap - leafRoom ||
@@ -897,14 +928,14 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
     if (!grid_barrier(c)) return;
     timeline_mark(c, ntiles);
 
-    // PLAN: one segment per CTA
+    // PLAN: one item (kThreads tiles of one segment) per CTA
     {
       unsigned* wc = &c->work[phase & 3];
       if (blockIdx.x == 0 && tid == 0) c->work[(phase + 2) & 3] = 0;
       for (;;) {
-        const int sgi = claim_item(wc);
-        if (sgi >= nsegs) break;
-        plan_segment<U, kIdx>(a, level, sgi, sm);
+        const int it = claim_item(wc);
+        if (it >= nplan) break;
+        plan_item<U, kIdx>(a, level, it, sm);
       }
       ++phase;
     }
@@ -917,6 +948,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
       // this level's list was read by everyone before the last barrier;
       // level+2 appends to it during the next PLAN phase
       st.store(0ull, cuda::memory_order_relaxed);
+      c->planCount[par] = 0;
       c->work[(phase + 2) & 3] = 0;
     }
     stream_tiles<U, kIdx, 1>(a, level, ntiles, &c->work[phase & 3], ws, mphase);
@@ -1112,7 +1144,8 @@ static cudaError_t prepare_persistent(int device, int* gridOut) {
 }
 
 template <typename U, bool kIdx>
-static cudaError_t launch_persistent(const SortArgs& a, int grid, cudaStream_t stream) {
+static cudaError_t launch_persistent(const SortArgs& a, int grid, cudaStream_t stream,
+                                     cudaEvent_t mid) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
   cfg.blockDim = dim3(kThreads);
@@ -1125,6 +1158,7 @@ static cudaError_t launch_persistent(const SortArgs& a, int grid, cudaStream_t s
   cfg.numAttrs = 1;
   cudaError_t e = cudaLaunchKernelEx(&cfg, persistent_sort_kernel<U, kIdx>, a);
   if (e != cudaSuccess) return e;
+  if (mid != nullptr && (e = cudaEventRecord(mid, stream)) != cudaSuccess) return e;
   int sms = 0, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1166,8 +1200,8 @@ cudaError_t kernels_prepare(int width, bool hasIdx, int device, int* grid) {
 }
 
 cudaError_t kernels_launch_persistent(int width, bool hasIdx, const SortArgs& a, int grid,
-                                      cudaStream_t stream) {
-  TURTLE_WIDTH_DISPATCH(width, hasIdx, (launch_persistent<U, I>(a, grid, stream)));
+                                      cudaStream_t stream, cudaEvent_t mid) {
+  TURTLE_WIDTH_DISPATCH(width, hasIdx, (launch_persistent<U, I>(a, grid, stream, mid)));
 }
 
 cudaError_t kernels_launch_multisort(int width, bool hasIdx, void* keys, int* idx,
