@@ -29,14 +29,17 @@ constexpr int kThreads = TURTLE_PART_THREADS;  // CTA size of the partition kern
 constexpr int kWarps = kThreads / 32;
 constexpr int kMinBlocks = TURTLE_PART_BLOCKS; // resident partition CTAs per SM we compile for
 #ifndef TURTLE_PART_TILE
-#define TURTLE_PART_TILE 4096
+#define TURTLE_PART_TILE 2048
 #endif
 constexpr int kPartTile = TURTLE_PART_TILE;  // partition tile (keys), a power of two
 constexpr int kLThreads = 512;           // CTA size of the leaf / batched kernels
 constexpr int kLWarps = kLThreads / 32;
 constexpr int kFillChunk = 1 << 16;      // pivot-run fill work unit (elements)
-constexpr int kDepthSwitch = 48;         // levels of start/mid/stop pivots before
-                                         // switching to sampled quartile pivots
+#ifndef TURTLE_DEPTH_SWITCH
+#define TURTLE_DEPTH_SWITCH 48
+#endif
+constexpr int kDepthSwitch = TURTLE_DEPTH_SWITCH;  // levels of start/mid/stop pivots
+                                         // before switching to sampled quartile pivots
 constexpr int kMaxLevels = 4096;         // hard cap on partition levels
 constexpr int kLeafClasses = 10;         // group sizes 1, 2, 4, ..., 512 threads
 constexpr long long kSpinLimit = 40000000LL;  // bounded barrier spin iterations

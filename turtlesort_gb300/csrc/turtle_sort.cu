@@ -532,36 +532,38 @@ __device__ __noinline__ void plan_item(const SortArgs& a, int level, int item,
     return;
   }
 
-  // item 0: children -- thread 0 routes them; the CTA writes the tile descriptors
+  // item 0: children -- thread c routes class c (fill, leaf or next-level
+  // segment); the CTA then writes the new segments' tile descriptors
   const bool dstIsA = (par == 1);
   const int nextPar = par ^ 1;
-  if (tid == 0) {
-    for (int c = 0; c < 7; ++c) {
-      const long long pos = sdStart + sm.cbase[c];
-      const long long m = sm.cbase[c + 1] - sm.cbase[c];
-      if (c & 1) {
-        if (m > 0 && !dstIsA) push_fill(a, pos, m, (unsigned long long)sm.piv[c >> 1]);
-        continue;
-      }
+  if (tid < 7) {
+    const int c = tid;
+    const long long pos = sdStart + sm.cbase[c];
+    const long long m = sm.cbase[c + 1] - sm.cbase[c];
+    if (c & 1) {
+      if (m > 0 && !dstIsA) push_fill(a, pos, m, (unsigned long long)sm.piv[c >> 1]);
+    } else {
       const int ci = c >> 1;
-      sm.childSeg[ci] = -1;
-      if (m <= 0 || (m == 1 && dstIsA)) continue;
-      if (m <= kLeafMax) {
-        push_leaf(a, pos, m, dstIsA ? 0 : 1);
-        continue;
+      int si = -1;
+      if (m > 1 || (m == 1 && !dstIsA)) {
+        if (m <= kLeafMax) {
+          push_leaf(a, pos, m, dstIsA ? 0 : 1);
+        } else {
+          int tb = 0, ntc = 0;
+          si = alloc_segment<kTile>(a, nextPar, pos, m, &tb, &ntc);
+          sm.childTb[ci] = tb;
+          sm.childNt[ci] = si >= 0 ? ntc : 0;
+          sm.childStart[ci] = pos;
+          sm.childN[ci] = m;
+        }
       }
-      int tb = 0, ntc = 0;
-      const int si = alloc_segment<kTile>(a, nextPar, pos, m, &tb, &ntc);
       sm.childSeg[ci] = si;
-      sm.childTb[ci] = tb;
-      sm.childNt[ci] = si >= 0 ? ntc : 0;
-      sm.childStart[ci] = pos;
-      sm.childN[ci] = m;
+      sdp->childSeg[ci] = si;
     }
-    for (int k = 0; k < 3; ++k) sdp->pivS[k] = (unsigned long long)sm.piv[k];
-    sdp->lut = sm.lut;
-    for (int c = 0; c < 8; ++c) sdp->cbase[c] = sdStart + sm.cbase[c];
-    for (int ci = 0; ci < 4; ++ci) sdp->childSeg[ci] = sm.childSeg[ci];
+    sdp->cbase[c] = pos;
+    if (c == 6) sdp->cbase[7] = sdStart + sm.cbase[7];
+    if (c < 3) sdp->pivS[c] = (unsigned long long)sm.piv[c];
+    if (c == 3) sdp->lut = sm.lut;
   }
   __syncthreads();
   for (int ci = 0; ci < 4; ++ci) {
