@@ -271,8 +271,13 @@ def batched(args):
 
 def serving(args):
     """A bounded sample of the serving stream: args.requests requests with
-    Poisson arrivals, log-uniform sizes in [1024, 16 * 2^20], dtype int32 60% /
-    int64 25% / uint16 15%, half with ids, HBM budget 64 GB."""
+    log-uniform sizes in [1024, 16 * 2^20], dtype int32 60% / int64 25% /
+    uint16 15%, half with ids, HBM budget 64 GB.  Three runs over the same
+    pre-filled pinned buffers (refilled, untimed, before each run):
+      serial      one StartSorting + Sync per request, back to back;
+      saturated   every request submitted at once to the server (throughput);
+      poisson     Poisson arrivals at half the saturated request rate
+                  (latency from arrival to completion: p50 / p99)."""
     torch = _torch()
     nreq = args.requests
     rng_u = dg.uniform_real(4 * nreq, dg.seed_for(4))
@@ -281,32 +286,41 @@ def serving(args):
     with_idx = rng_u[2 * nreq:3 * nreq] < 0.5
     dtypes = [np.int32, np.int64, np.uint16]
     pool = dg.uniform(np.uint64, 1 << 25, dg.seed_for(4) + 1)  # 256 MiB of random words
-    maxb = int(sizes.max()) * 8
-    nslots = 12
-    slot_k = [torch.empty(maxb, dtype=torch.uint8, pin_memory=True) for _ in range(nslots)]
-    slot_i = [torch.empty(int(sizes.max()) * 4, dtype=torch.uint8, pin_memory=True)
-              for _ in range(nslots)]
-
-    def fill(r, slot):
+    keys_total = int(sizes.sum())
+    kb = [int(sizes[r]) * np.dtype(dtypes[dts[r]]).itemsize for r in range(nreq)]
+    ib = [int(sizes[r]) * 4 if with_idx[r] else 0 for r in range(nreq)]
+    koff = np.concatenate([[0], np.cumsum([(x + 15) // 16 * 16 for x in kb])])
+    ioff = np.concatenate([[0], np.cumsum([(x + 15) // 16 * 16 for x in ib])])
+    arena_k = torch.empty(int(koff[-1]), dtype=torch.uint8, pin_memory=True)
+    arena_i = torch.empty(max(int(ioff[-1]), 16), dtype=torch.uint8, pin_memory=True)
+    ak, ai = arena_k.numpy(), arena_i.numpy()
+    views = []
+    for r in range(nreq):
         dt = np.dtype(dtypes[dts[r]])
         n = int(sizes[r])
-        words = (n * dt.itemsize + 7) // 8
-        off = int((r * 7919) % (pool.size - words))
-        kv = slot_k[slot].numpy()[: n * dt.itemsize].view(dt)
-        kv[:] = pool[off: off + words].view(dt)[:n]
-        iv = None
-        if with_idx[r]:
-            iv = slot_i[slot].numpy()[: n * 4].view(np.int32)
-            iv[:] = np.arange(n, dtype=np.int32)
-        return kv, iv
+        kv = ak[koff[r]: koff[r] + kb[r]].view(dt)
+        iv = ai[ioff[r]: ioff[r] + ib[r]].view(np.int32) if with_idx[r] else None
+        views.append((kv, iv))
 
-    # serial baseline: one StartSorting + Sync per request, back to back
+    def refill():
+        for r, (kv, iv) in enumerate(views):
+            words = (kv.nbytes + 7) // 8
+            off = int((r * 7919) % (pool.size - words))
+            kv[:] = pool[off: off + words].view(kv.dtype)[: kv.size]
+            if iv is not None:
+                iv[:] = np.arange(iv.size, dtype=np.int32)
+
+    def check():
+        for r, (kv, iv) in enumerate(views):
+            if kv.size > 1 and not np.all(kv[:-1] <= kv[1:]):
+                raise RuntimeError(f"request {r} not sorted")
+
+    # serial baseline
+    refill()
     sorters = {}
     t_serial = 0.0
-    keys_total = int(sizes.sum())
-    for r in range(nreq):
-        kv, iv = fill(r, 0)
-        key = (dts[r], bool(with_idx[r]))
+    for r, (kv, iv) in enumerate(views):
+        key = (int(dts[r]), iv is not None)
         if key not in sorters:
             sorters[key] = ts.TurtleSort(dtypes[dts[r]], int(sizes.max()), track_index=key[1])
         t0 = time.perf_counter()
@@ -315,73 +329,71 @@ def serving(args):
         t_serial += time.perf_counter() - t0
     for s in sorters.values():
         s.close()
+    check()
     serial_kps = keys_total / t_serial
-    # Poisson arrivals offering 1.5x the serial rate
-    rate = args.rate if args.rate > 0 else 1.5 * nreq / t_serial
+
+    srv = ts.TurtleServer(hbm_budget_bytes=64 << 30)
+    # warm the server's pool and kernels with one pass, untimed
+    refill()
+    for t in [srv.submit(kv, iv) for kv, iv in views[: min(8, nreq)]]:
+        srv.wait(t)
+    # saturated: everything submitted at once
+    refill()
+    t0 = time.perf_counter()
+    tickets = [srv.submit(kv, iv) for kv, iv in views]
+    for t in tickets:
+        srv.wait(t)
+    t_sat = time.perf_counter() - t0
+    check()
+    sat_kps = keys_total / t_sat
+    # Poisson arrivals at half the saturated request rate
+    rate = args.rate if args.rate > 0 else 0.5 * nreq / t_sat
     gaps = -np.log(np.maximum(rng_u[3 * nreq:4 * nreq], 1e-12)) / rate
     arrivals = np.cumsum(gaps)
-    free = list(range(nslots))
+    refill()
+    lat = [0.0] * nreq
+    done_q = []
     cv = threading.Condition()
-    lat = []
-    pending = []
-    srv = ts.TurtleServer(hbm_budget_bytes=64 << 30)
 
     def waiter():
-        while True:
+        for r in range(nreq):
             with cv:
-                while not pending:
+                while len(done_q) <= r:
                     cv.wait()
-                item = pending.pop(0)
-            if item is None:
-                return
-            r, ticket, slot, kv, t_arr = item
+                ticket, t_arr = done_q[r]
             srv.wait(ticket)
-            done = time.perf_counter()
-            if kv.size > 1 and not np.all(kv[:-1] <= kv[1:]):
-                raise RuntimeError(f"request {r} not sorted")
-            with cv:
-                lat.append(done - t_arr)
-                free.append(slot)
-                cv.notify_all()
+            lat[r] = time.perf_counter() - t_arr
 
     th = threading.Thread(target=waiter)
     th.start()
     t_start = time.perf_counter()
-    for r in range(nreq):
+    for r, (kv, iv) in enumerate(views):
         target = t_start + arrivals[r]
         now = time.perf_counter()
         if target > now:
             time.sleep(target - now)
-        with cv:
-            while not free:
-                cv.wait()
-            slot = free.pop()
-        kv, iv = fill(r, slot)
         ticket = srv.submit(kv, iv)
         with cv:
-            pending.append((r, ticket, slot, kv, max(target, t_start)))
+            done_q.append((ticket, max(target, t_start)))
             cv.notify_all()
-    with cv:
-        pending.append(None)
-        cv.notify_all()
     th.join()
-    t_total = time.perf_counter() - t_start
+    t_pois = time.perf_counter() - t_start
+    check()
     st = srv.stats()
     srv.close()
     lat_ms = np.array(lat) * 1e3
-    _line("served keys/s (Poisson request stream, continuous batching)", keys_total / t_total,
-          "keys/s", args,
+    _line("served keys/s (request stream, continuous batching, saturated)", sat_kps, "keys/s", args,
           {"workload": f"{nreq} requests (bounded sample of 20,000), sizes log-uniform "
                        f"[1024, 16*2^20], int32 60%/int64 25%/uint16 15%, half with ids, "
-                       f"HBM budget 64 GB", "requests": nreq, "keys": keys_total,
-           "arrival_rate_per_s": rate},
-          {"dtype": "mixed", "p50_ms": float(np.percentile(lat_ms, 50)),
-           "p99_ms": float(np.percentile(lat_ms, 99)),
-           "server_p50_ms": st["p50_ms"], "server_p99_ms": st["p99_ms"],
-           "batches": st["batches"], "serial_startsorting_keys_per_s": serial_kps,
-           "speedup_vs_serial": (keys_total / t_total) / serial_kps,
-           "e2e": {"value": keys_total / t_total, "unit": "keys/s",
-                   "note": "host buffers pinned; copies inside every request's latency"}})
+                       f"HBM budget 64 GB", "requests": nreq, "keys": keys_total},
+          {"dtype": "mixed",
+           "poisson": {"arrival_rate_per_s": rate, "p50_ms": float(np.percentile(lat_ms, 50)),
+                       "p99_ms": float(np.percentile(lat_ms, 99)),
+                       "keys_per_s": keys_total / t_pois},
+           "batches_total": st["batches"], "serial_startsorting_keys_per_s": serial_kps,
+           "speedup_vs_serial": sat_kps / serial_kps,
+           "e2e": {"value": sat_kps, "unit": "keys/s",
+                   "note": "pinned host buffers; host<->device copies inside every request"}})
 
 
 WORKLOADS = {"plain12m": plain12m, "sweep": sweep, "wide": wide, "multisort": multisort,

@@ -242,6 +242,13 @@ turtle_status turtle_debug_time_kernels(turtle_sorter* s, int enable);
  * sorts.  Returns the number of sorts summed (0 if timing is off). */
 int turtle_debug_kernel_times(turtle_sorter* s, int last, double* partition_ms, double* leaf_ms);
 
+/* Where the last sort's device-side error was recorded (valid after
+ * turtle_stream_status / turtle_sync): site 1 = grid barrier wait limit,
+ * 2 = grid barrier (with leaf work) wait limit, 3 = bulk-copy wait limit,
+ * 4 = a work list was full; block = the CTA; info = site detail.  Returns
+ * the device status word (0 = no error). */
+int turtle_debug_error_site(const turtle_sorter* s, int* site, int* block, int* info);
+
 /* Library version string (static storage). */
 const char* turtle_version(void);
 

@@ -64,12 +64,21 @@ def _stream(stream) -> Optional[C.c_void_p]:
     return C.c_void_p(CUDA_STREAM_LEGACY if int(stream) == 0 else int(stream))
 
 
+_SITES = {1: "grid barrier wait", 3: "bulk-copy wait", 4: "work list full"}
+
+
 def _check(st: int, where: str, handle=None) -> None:
     if st != 0:
         detail = ""
         if handle is not None:
-            raw = load_library().turtle_last_cuda_error(handle)
+            lib = load_library()
+            raw = lib.turtle_last_cuda_error(handle)
             detail = raw.decode() if raw else ""
+            if st in (5, 6):  # device-side: say which wait or list
+                site, block, info = C.c_int(), C.c_int(), C.c_int()
+                lib.turtle_debug_error_site(handle, C.byref(site), C.byref(block), C.byref(info))
+                detail = (f"{_SITES.get(site.value, site.value)} in block {block.value}, "
+                          f"info {info.value}")
         raise TurtleError(st, where, detail)
 
 
@@ -202,6 +211,13 @@ class TurtleSort:
     @property
     def last_levels(self) -> int:
         return int(self._lib.turtle_last_levels(self._h))
+
+    def error_site(self):
+        """(device status, site, block, info) of the last sort's device-side error."""
+        site, block, info = C.c_int(), C.c_int(), C.c_int()
+        st = self._lib.turtle_debug_error_site(self._h, C.byref(site), C.byref(block),
+                                               C.byref(info))
+        return int(st), int(site.value), int(block.value), int(info.value)
 
     def time_kernels(self, enable: bool = True) -> None:
         """Record CUDA events around the partition and leaf kernels of every

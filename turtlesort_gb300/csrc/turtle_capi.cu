@@ -540,6 +540,14 @@ int turtle_debug_kernel_times(turtle_sorter* s, int last, double* partition_ms, 
   return (int)n;
 }
 
+int turtle_debug_error_site(const turtle_sorter* s, int* site, int* block, int* info) {
+  if (!s || !s->hctrl) return 0;
+  if (site) *site = s->hctrl->errSite;
+  if (block) *block = s->hctrl->errBlock;
+  if (info) *info = s->hctrl->errInfo;
+  return s->hctrl->error;
+}
+
 const char* turtle_version(void) { return "turtle-gb300 0.1 (sm_103a)"; }
 
 }  // extern "C"

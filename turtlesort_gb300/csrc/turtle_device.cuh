@@ -143,6 +143,9 @@ struct Control {
   int yield;                      // 1: partition stopped early to drain the leaf lists
   int resumeLevel;                // level to continue from after a yield
   int resumePhase;                // work-counter ring position at the yield
+  int errSite;                    // which bounded wait or check recorded `error`
+  int errBlock;                   // the CTA that recorded it
+  int errInfo;                    // site-specific detail
   unsigned long long tEnd;        // globaltimer when the last CTA finished
   unsigned long long tl[kTimeline];  // globaltimer (ns) after each grid barrier
   int tlInfo[kTimeline];             // work items of the phase that just ended
@@ -180,10 +183,19 @@ __device__ __forceinline__ int ld_acquire_int(int* p) {
   cuda::atomic_ref<int, cuda::thread_scope_device> a(*p);
   return a.load(cuda::memory_order_acquire);
 }
-__device__ __forceinline__ void set_error(Control* c, int code) {
+// Error sites recorded with the first error (Control::errSite).
+constexpr int kSiteBarrier = 1;    // grid_barrier spin limit
+constexpr int kSiteBulk = 3;       // bulk-copy barrier wait limit
+constexpr int kSiteCapacity = 4;   // a work list was full
+
+__device__ __forceinline__ void set_error(Control* c, int code, int site = 0, int info = 0) {
   cuda::atomic_ref<int, cuda::thread_scope_device> a(c->error);
   int expected = 0;
-  a.compare_exchange_strong(expected, code, cuda::memory_order_acq_rel);
+  if (a.compare_exchange_strong(expected, code, cuda::memory_order_acq_rel)) {
+    c->errSite = site;
+    c->errBlock = (int)blockIdx.x;
+    c->errInfo = info;
+  }
 }
 
 // Grid-wide barrier for a cooperatively launched grid.  The spin is bounded:
@@ -207,7 +219,7 @@ __device__ __forceinline__ bool grid_barrier(Control* c) {
       while (gen.load(cuda::memory_order_acquire) == g) {
         if (ld_acquire_int(&c->error) != 0) break;
         if (++it > kSpinLimit) {
-          set_error(c, kDevTimeout);
+          set_error(c, kDevTimeout, kSiteBarrier, (int)g);
           break;
         }
         __nanosleep(ns);
@@ -413,17 +425,20 @@ __device__ __forceinline__ int class_lut(KT k, KT p1, KT p2, KT p3, unsigned lut
 // elements in registers by odd-even transposition (stable), then log2(P)
 // rounds of merge-path merges (ties taken from the left run) produce the
 // sorted group.  Results are left in shared memory.  All threads of the CTA
-// must call it (it synchronizes).
+// must call it (it synchronizes); only threads below `active` (a multiple of
+// P) touch the arrays, so a CTA whose size is not a multiple of P sorts its
+// complete groups and its remaining threads only take part in the barriers.
 template <typename KT, int kItems, bool kIdx>
-__device__ __forceinline__ void block_sort_groups(KT* sk, int* si, int P) {
+__device__ __forceinline__ void block_sort_groups(KT* sk, int* si, int P, int active) {
   const int tid = threadIdx.x;
+  const bool on = tid < active;
   KT k[kItems];
   int v[kItems];
   const int base = tid * kItems;
 #pragma unroll
   for (int i = 0; i < kItems; ++i) {
-    k[i] = sk[kpad<KT>(base + i)];
-    if (kIdx) v[i] = si[ipad(base + i)];
+    k[i] = on ? sk[kpad<KT>(base + i)] : KT(0);
+    if (kIdx) v[i] = on ? si[ipad(base + i)] : 0;
   }
   // odd-even transposition: swap only on strict inversion -> stable
 #pragma unroll
@@ -441,12 +456,15 @@ __device__ __forceinline__ void block_sort_groups(KT* sk, int* si, int P) {
   for (int w = 1; w < P; w <<= 1) {
     // registers -> smem (blocked)
     __syncthreads();
+    if (on) {
 #pragma unroll
-    for (int i = 0; i < kItems; ++i) {
-      sk[kpad<KT>(base + i)] = k[i];
-      if (kIdx) si[ipad(base + i)] = v[i];
+      for (int i = 0; i < kItems; ++i) {
+        sk[kpad<KT>(base + i)] = k[i];
+        if (kIdx) si[ipad(base + i)] = v[i];
+      }
     }
     __syncthreads();
+    if (!on) continue;
     // merge runs of w threads pairwise: my pair starts at thread pf
     const int pair_lane = lane_in_group & (2 * w - 1);
     const int pf = tid - pair_lane;
@@ -483,10 +501,12 @@ __device__ __forceinline__ void block_sort_groups(KT* sk, int* si, int P) {
   }
   (void)group_first;
   __syncthreads();
+  if (on) {
 #pragma unroll
-  for (int i = 0; i < kItems; ++i) {
-    sk[kpad<KT>(base + i)] = k[i];
-    if (kIdx) si[ipad(base + i)] = v[i];
+    for (int i = 0; i < kItems; ++i) {
+      sk[kpad<KT>(base + i)] = k[i];
+      if (kIdx) si[ipad(base + i)] = v[i];
+    }
   }
   __syncthreads();
 }

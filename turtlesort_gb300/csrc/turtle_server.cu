@@ -83,6 +83,7 @@ struct turtle_server {
   int maxBatchRequests = 4096;
   long long maxBatchKeys = 32ll << 20;
   cudaStream_t sIn = nullptr, sSort = nullptr, sOut = nullptr;
+  cudaMemPool_t pool = nullptr;  // the server's own stream-ordered pool (keeps freed batches)
   int grid[9][2] = {};
   Slot slots[kSlots];
   std::mutex mu;
@@ -126,7 +127,7 @@ void fail_request(turtle_server* s, Request* r, turtle_status st) {
 turtle_status launch_batch(turtle_server* s, Batch* b) {
   Slot& sl = s->slots[b->slot];
   const long long num = (long long)b->reqs.size();
-  cudaError_t e = cudaMallocAsync((void**)&b->dev, b->bytes, s->sIn);
+  cudaError_t e = cudaMallocFromPoolAsync((void**)&b->dev, b->bytes, s->pool, s->sIn);
   if (e != cudaSuccess) { cudaGetLastError(); return TURTLE_ERR_OUT_OF_MEMORY; }
   const size_t kb = turtle::align_up((size_t)b->total * b->width + 16, 256);
   const size_t ib = b->hasIdx ? turtle::align_up((size_t)b->total * 4 + 16, 256) : 0;
@@ -351,6 +352,19 @@ turtle_status turtle_server_create(int device, int64_t hbm_budget_bytes, int max
   cudaError_t e = cudaSuccess;
   for (int w : {1, 2, 4, 8})
     for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = turtle::kernels_prepare(w, i != 0, device, &s->grid[w][i]);
+  if (e == cudaSuccess) {
+    // a private pool whose freed blocks stay mapped up to the budget, so a
+    // steady request stream does not map and unmap device memory per batch
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    e = cudaMemPoolCreate(&s->pool, &props);
+    if (e == cudaSuccess) {
+      unsigned long long keep = (unsigned long long)hbm_budget_bytes;
+      e = cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+  }
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->sIn, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->sSort, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->sOut, cudaStreamNonBlocking);
@@ -479,6 +493,7 @@ turtle_status turtle_server_destroy(turtle_server* s) {
     if (sl.hOffs) cudaFreeHost(sl.hOffs);
     if (sl.hCtrl) cudaFreeHost(sl.hCtrl);
   }
+  if (s->pool) cudaMemPoolDestroy(s->pool);
   if (s->sIn) cudaStreamDestroy(s->sIn);
   if (s->sSort) cudaStreamDestroy(s->sSort);
   if (s->sOut) cudaStreamDestroy(s->sOut);

@@ -184,7 +184,7 @@ __device__ int alloc_segment(const SortArgs& a, int par, long long start, long l
   const int np = (int)((nt + kThreads - 1) / kThreads);  // plan items
   const int pb = atomicAdd(&a.ctrl->planCount[par], np);
   if (si >= a.segCap || tb + nt > a.tileCap || pb + np > a.planCap) {
-    set_error(a.ctrl, kDevCapacity);
+    set_error(a.ctrl, kDevCapacity, kSiteCapacity, 1);
     return -1;
   }
   SegDesc d;
@@ -231,7 +231,7 @@ __device__ __forceinline__ TileDesc load_tile(const TileDesc* p) {
 
 __device__ void push_leaf(const SortArgs& a, long long start, long long n, int inB) {
   const int li = atomicAdd(&a.ctrl->leafCount, 1);
-  if (li >= a.leafCap) { set_error(a.ctrl, kDevCapacity); return; }
+  if (li >= a.leafCap) { set_error(a.ctrl, kDevCapacity, kSiteCapacity, 2); return; }
   LeafDesc d;
   d.start = start; d.n = (int)n; d.inB = inB;
   a.leaves[li] = d;
@@ -240,7 +240,7 @@ __device__ void push_leaf(const SortArgs& a, long long start, long long n, int i
 __device__ void push_fill(const SortArgs& a, long long start, long long n, unsigned long long v) {
   for (long long o = 0; o < n; o += kFillChunk) {
     const int fi = atomicAdd(&a.ctrl->fillCount, 1);
-    if (fi >= a.fillCap) { set_error(a.ctrl, kDevCapacity); return; }
+    if (fi >= a.fillCap) { set_error(a.ctrl, kDevCapacity, kSiteCapacity, 3); return; }
     FillDesc d;
     d.start = start + o;
     d.n = (int)((n - o) < kFillChunk ? (n - o) : kFillChunk);
@@ -354,7 +354,8 @@ __device__ __forceinline__ void chunk_keys(const typename Persist<U, kIdx>::Warp
 template <typename U, bool kIdx>
 __device__ __forceinline__ void chunk_wait(typename Persist<U, kIdx>::WarpArea& ws, int b,
                                            unsigned& phases, Control* c) {
-  if (!mbar_wait(&ws.mbar[b], (phases >> b) & 1u)) set_error(c, kDevTimeout);
+  if (!mbar_wait(&ws.mbar[b], (phases >> b) & 1u))
+    set_error(c, kDevTimeout, kSiteBulk, (int)(threadIdx.x >> 5) * 16 + b * 2 + (int)((phases >> b) & 1u));
   phases ^= 1u << b;
 }
 
@@ -994,7 +995,7 @@ __device__ void sort_leaf_group(const SortArgs& a, int cls, int first, int last,
   }
   __syncthreads();
   if (!kRadixLeaves || cls <= kMergeClassMax)
-    block_sort_groups<KT, kItems, kIdx>(sm.keys, sm.idx, P);
+    block_sort_groups<KT, kItems, kIdx>(sm.keys, sm.idx, P, kLThreads);
   else
     group_radix_sort<KT, kItems, kIdx, kLWarps>(sm.keys, sm.idx, d.n, P >> 5, sm.rcnt, sm.rred,
                                                 &sm.rpass);
@@ -1103,7 +1104,7 @@ __global__ void __launch_bounds__(kLThreads, 2)
   }
   __syncthreads();
   if (!kRadixLeaves || cls <= kMergeClassMax) {
-    block_sort_groups<KT, kItems, kIdx>(sm.keys, sm.idx, P);
+    block_sort_groups<KT, kItems, kIdx>(sm.keys, sm.idx, P, kLThreads);
   } else {
     const int g = tid / P;
     group_radix_sort<KT, kItems, kIdx, kLWarps>(sm.keys, sm.idx, g < na ? arrSize : 0, P >> 5,
