@@ -196,6 +196,16 @@ turtle_status turtle_server_get_stats(turtle_server* srv, turtle_server_stats* o
  * the server.  Safe on NULL. */
 turtle_status turtle_server_destroy(turtle_server* srv);
 
+/* Pivot rule of this sorter (no counterpart in the reference; the output is
+ * the same either way because every step is stable):
+ *   TURTLE_PIVOTS_REFERENCE  sorted{a[start+n/2], a[start], a[stop]} per
+ *                            segment, as the reference (turtle-sort.cu:641-655);
+ *   TURTLE_PIVOTS_SAMPLED    the quartiles of 15 evenly spaced keys of the
+ *                            segment (default): fewer partition levels. */
+#define TURTLE_PIVOTS_REFERENCE 0
+#define TURTLE_PIVOTS_SAMPLED 1
+turtle_status turtle_set_pivot_rule(turtle_sorter* s, int rule);
+
 /* ---- introspection ---- */
 
 /* Kernel launches issued by this sorter since it was created. */

@@ -198,3 +198,25 @@ def test_errors():
     h = np.zeros(10 * 33, dtype=np.int32)
     with pytest.raises(TurtleError):
         s.MultiSort(10, 33, h, block_size=32)  # 33 % 32 != 0, as the reference requires
+
+
+@pytest.mark.parametrize("dtype", [np.int32, np.uint8, np.int64, np.uint16])
+def test_pivot_rules_give_the_same_result(dtype):
+    """The reference pivot rule (median of start/middle/stop) and the sampled
+    rule (quartiles of 15 evenly spaced keys) must both produce the stable
+    order: pivots shape the partition tree, never the output."""
+    n = 700_001
+    for dist, seed in [("uniform", 4), ("dups", 5), ("sorted", 6), ("organ", 7)]:
+        k = make_keys(dtype, n, dist, seed)
+        idx = np.arange(n, dtype=np.int32)
+        outs = []
+        for rule in ("reference", "sampled"):
+            s = TurtleSort(dtype, n, track_index=True)
+            s.set_pivot_rule(rule)
+            ko, io = k.copy(), idx.copy()
+            s.StartSorting(ko, io)
+            s.Sync()
+            s.close()
+            check_sorted_pair(k, ko, io, idx)
+            outs.append((ko, io))
+        assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])

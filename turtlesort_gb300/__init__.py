@@ -212,6 +212,12 @@ class TurtleSort:
     def last_levels(self) -> int:
         return int(self._lib.turtle_last_levels(self._h))
 
+    def set_pivot_rule(self, rule: str) -> None:
+        """'sampled' (default: quartiles of 15 evenly spaced keys) or 'reference'
+        (the reference's median of start/middle/stop keys); same output."""
+        code = {"reference": 0, "sampled": 1}[rule]
+        _check(self._lib.turtle_set_pivot_rule(self._h, code), "set_pivot_rule", self._h)
+
     def error_site(self):
         """(device status, site, block, info) of the last sort's device-side error."""
         site, block, info = C.c_int(), C.c_int(), C.c_int()

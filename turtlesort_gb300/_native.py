@@ -54,6 +54,7 @@ SIGNATURES = [
     ("turtle_debug_timeline", _I, [_P, _P, _P, _I]),
     ("turtle_sort_device_noalloc", _I, [_I, _P, _P, _I64, _P]),
     ("turtle_noalloc_max_elements", _I64, []),
+    ("turtle_set_pivot_rule", _I, [_P, _I]),
     ("turtle_debug_time_kernels", _I, [_P, _I]),
     ("turtle_debug_kernel_times", _I, [_P, _I, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("turtle_debug_error_site", _I, [_P, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I)]),

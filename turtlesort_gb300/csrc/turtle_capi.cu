@@ -66,6 +66,7 @@ struct turtle_sorter {
   bool lastHasIdx = false;
   bool lastValid = false;
   cudaStream_t lastStream = nullptr;
+  int pivotRule = turtle::kRuleSampled;
   // optional kernel timing: events around the two launches of each sort
   static constexpr int kRing = 64;
   bool timeKernels = false;
@@ -106,7 +107,7 @@ turtle_status alloc_workspace(turtle_sorter* s, long long extraLeaves) {
 turtle::SortArgs make_args(turtle_sorter* s, void* keys, int32_t* idx, const long long* offs,
                            long long num, long long n) {
   return turtle::bind_args(keys, idx, s->keysB.ptr, (int*)s->idxB.ptr, (char*)s->ws.ptr, s->lay,
-                           offs, num, n, s->flip);
+                           offs, num, n, s->flip, s->pivotRule);
 }
 
 // Enqueue: reset the control block, run the persistent kernel, copy the
@@ -506,6 +507,15 @@ int turtle_debug_timeline(const turtle_sorter* s, uint64_t* ns, int32_t* info, i
   ns[n] = s->hctrl->tEnd;
   info[n] = -2;
   return n + 1;
+}
+
+turtle_status turtle_set_pivot_rule(turtle_sorter* s, int rule) {
+  if (!s || (rule != turtle::kRuleReference && rule != turtle::kRuleSampled))
+    return TURTLE_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(s->mu);
+  free_graphs(s);  // captured launches hold the old rule
+  s->pivotRule = rule;
+  return TURTLE_OK;
 }
 
 turtle_status turtle_debug_time_kernels(turtle_sorter* s, int enable) {

@@ -41,6 +41,7 @@ constexpr int kFillChunk = 1 << 16;      // pivot-run fill work unit (elements)
 constexpr int kDepthSwitch = TURTLE_DEPTH_SWITCH;  // levels of start/mid/stop pivots
                                          // before switching to sampled quartile pivots
 constexpr int kMaxLevels = 4096;         // hard cap on partition levels
+constexpr int kSamples = 15;             // evenly spaced pivot samples (sampled rule)
 constexpr int kLeafClasses = 10;         // group sizes 1, 2, 4, ..., 512 threads
 constexpr long long kSpinLimit = 40000000LL;  // bounded barrier spin iterations
 constexpr int kTimeline = 160;           // phase timestamps kept per launch
@@ -91,8 +92,10 @@ struct SegDesc {        // a segment partitioned by the multi-CTA 3-pivot pass
   long long n;
   int tileBase;         // first entry in this level's tile arrays
   int ntiles;
-  unsigned long long piv[3];   // pivot candidates a[start+n/2], a[start], a[stop]
-                               // (unsigned images; captured by the parent's scatter)
+  unsigned long long samp[16]; // pivot samples (unsigned images; captured by the
+                               // parent's scatter): a[start+n/2], a[start], a[stop]
+                               // under the reference rule, else kSamples evenly
+                               // spaced keys
   unsigned long long pivS[3];  // sorted pivots (unsigned images), set by the plan
   unsigned lut;         // class remap for equal pivots, set by the plan
   int pad;
@@ -171,6 +174,7 @@ struct SortArgs {
   FillDesc* fills;
   int segCap, tileCap, leafCap, fillCap, planCap;
   int resume;                // 1: continue a partition that yielded
+  int samples;               // pivot samples per segment: 3 (reference rule) or kSamples
   Control* ctrl;
 };
 

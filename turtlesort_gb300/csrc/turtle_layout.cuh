@@ -72,9 +72,16 @@ inline unsigned long long dtype_flip(int dt) {
 
 // Kernel arguments for sorting `keys` (+ `idx`) with scratch buffers
 // keysB / idxB and the work lists laid out by L inside `ws`.
+// Pivot rules: the reference's median of a[start+n/2], a[start], a[stop]
+// (3 samples) or the quartiles of kSamples evenly spaced samples.  Both give
+// the same output (every step is stable); the sampled rule needs fewer levels.
+constexpr int kRuleReference = 0;
+constexpr int kRuleSampled = 1;
+inline int rule_samples(int rule) { return rule == kRuleReference ? 3 : kSamples; }
+
 inline SortArgs bind_args(void* keys, int* idx, void* keysB, int* idxB, char* ws, const WsLayout& L,
                           const long long* offs, long long num, long long n,
-                          unsigned long long flip) {
+                          unsigned long long flip, int rule = kRuleSampled) {
   SortArgs a;
   std::memset(&a, 0, sizeof(a));
   a.keysA = keys;
@@ -101,6 +108,7 @@ inline SortArgs bind_args(void* keys, int* idx, void* keysB, int* idxB, char* ws
   a.fillCap = L.fillCap;
   a.planCap = L.planCap;
   a.ctrl = (Control*)(ws + L.offCtrl);
+  a.samples = rule_samples(rule);
   return a;
 }
 

@@ -80,8 +80,8 @@ struct Persist {
     unsigned char sc[kWCH];         // class of each stage slot
     long long delta[8];             // destination minus stage slot, per class
     long long wbase[8];             // running destination per class
-    long long cpos[12];             // children's pivot positions (-1: none)
-    int cseg[12];                   // the child segment of each position
+    long long cpos[4][16];          // children's pivot sample positions
+    int cseg[4];                    // the child segments (-1: none)
     unsigned long long mbar[2];     // bulk-copy completion barriers
   };
 
@@ -153,16 +153,65 @@ __device__ __noinline__ void sampled_pivots(const U* src, long long start, long 
   piv[0] = s[7]; piv[1] = s[15]; piv[2] = s[23];
 }
 
-// Sorted pivots of a segment: its captured candidates on shallow levels,
-// samples of its keys on deep ones.
+// Position of pivot sample i of a segment [start, start+n): the reference's
+// a[start+n/2], a[start], a[stop] (turtle-sort.cu:641-655) for 3 samples,
+// else evenly spaced keys.
+__device__ __forceinline__ long long sample_pos(long long start, long long n, int i, int ns) {
+  if (ns == 3) return i == 0 ? start + n / 2 : i == 1 ? start : start + n - 1;
+  return start + ((2 * (long long)i + 1) * n) / (2 * ns);
+}
+
+// Sorted pivots of a segment: from its captured samples on shallow levels
+// (the sorted three under the reference rule, else the quartiles of the
+// kSamples samples), from samples of its keys on deep ones.
 template <typename KT, typename U>
 __device__ __forceinline__ void segment_pivots(const SegDesc* sd, const U* src, int level, KT flip,
-                                               KT* piv) {
-  if (level < kDepthSwitch) {
-    sort3<KT>((KT)__ldcg(&sd->piv[0]), (KT)__ldcg(&sd->piv[1]), (KT)__ldcg(&sd->piv[2]), piv);
-  } else {
+                                               int ns, KT* piv) {
+  if (level >= kDepthSwitch) {
     sampled_pivots<KT, U>(src, __ldcg(&sd->start), __ldcg(&sd->n), flip, piv);
+  } else if (ns == 3) {
+    sort3<KT>((KT)__ldcg(&sd->samp[0]), (KT)__ldcg(&sd->samp[1]), (KT)__ldcg(&sd->samp[2]), piv);
+  } else {
+    KT v[kSamples];
+#pragma unroll
+    for (int i = 0; i < kSamples; ++i) v[i] = (KT)__ldcg(&sd->samp[i]);
+    // rank of each sample (ties by index): the ranks 3, 7, 11 are the quartiles
+#pragma unroll
+    for (int i = 0; i < kSamples; ++i) {
+      int r = 0;
+#pragma unroll
+      for (int j = 0; j < kSamples; ++j) r += (v[j] < v[i]) || (v[j] == v[i] && j < i);
+      if (r == 3) piv[0] = v[i];
+      if (r == 7) piv[1] = v[i];
+      if (r == 11) piv[2] = v[i];
+    }
   }
+}
+
+// segment_pivots for a whole warp: the kSamples samples are ranked one per
+// lane with shuffles instead of by every lane.
+template <typename KT, typename U>
+__device__ __forceinline__ void segment_pivots_warp(const SegDesc* sd, const U* src, int level,
+                                                    KT flip, int ns, KT* piv) {
+  if (level >= kDepthSwitch || ns == 3) {
+    segment_pivots<KT, U>(sd, src, level, flip, ns, piv);
+    return;
+  }
+  const int lane = threadIdx.x & 31;
+  const KT v = lane < kSamples ? (KT)__ldcg(&sd->samp[lane]) : KT(0);
+  int r = 0;
+#pragma unroll
+  for (int j = 0; j < kSamples; ++j) {
+    const KT w = __shfl_sync(kFull, v, j);
+    r += (w < v) || (w == v && j < lane);
+  }
+  const bool in = lane < kSamples;
+  const int l1 = __ffs(__ballot_sync(kFull, in && r == 3)) - 1;
+  const int l2 = __ffs(__ballot_sync(kFull, in && r == 7)) - 1;
+  const int l3 = __ffs(__ballot_sync(kFull, in && r == 11)) - 1;
+  piv[0] = __shfl_sync(kFull, v, l1);
+  piv[1] = __shfl_sync(kFull, v, l2);
+  piv[2] = __shfl_sync(kFull, v, l3);
 }
 
 template <int kTile>
@@ -189,7 +238,7 @@ __device__ int alloc_segment(const SortArgs& a, int par, long long start, long l
   }
   SegDesc d;
   d.start = start; d.n = n; d.tileBase = (int)tb; d.ntiles = (int)nt;
-  d.piv[0] = d.piv[1] = d.piv[2] = 0;
+  for (int i = 0; i < 16; ++i) d.samp[i] = 0;
   d.pivS[0] = d.pivS[1] = d.pivS[2] = 0;
   d.lut = 0; d.pad = 0;
   for (int c = 0; c < 8; ++c) { d.cbase[c] = 0; d.tot[c] = 0; }
@@ -267,9 +316,8 @@ __device__ void route_input(const SortArgs& a, long long start, long long n, boo
   const U* src = (const U*)a.keysA;
   const KT flip = (KT)a.flip;
   SegDesc* sd = &a.segs[0][si];
-  sd->piv[0] = (unsigned long long)kload<U, KT>(src, start + n / 2, flip);
-  sd->piv[1] = (unsigned long long)kload<U, KT>(src, start, flip);
-  sd->piv[2] = (unsigned long long)kload<U, KT>(src, start + n - 1, flip);
+  for (int i = 0; i < a.samples; ++i)
+    sd->samp[i] = (unsigned long long)kload<U, KT>(src, sample_pos(start, n, i, a.samples), flip);
   if (writeTiles) write_tiles<kTile>(a, 0, si, tb, nt, start, n, 0, 1);
   *siOut = si; *tbOut = tb; *ntOut = nt;
 }
@@ -381,7 +429,7 @@ __device__ __forceinline__ void count_tile_warp(const SortArgs& a, int level, in
   const long long abs0 = (td.lo >> kShift) << kShift;
   const int rlo = (int)(td.lo - abs0), rhi = (int)(td.hi - abs0);
   KT piv[3];
-  segment_pivots<KT, U>(&a.segs[par][td.seg], src, level, flip, piv);
+  segment_pivots_warp<KT, U>(&a.segs[par][td.seg], src, level, flip, a.samples, piv);
   const int chBeg = rlo / kWCH, chEnd = (rhi + kWCH - 1) / kWCH;
   if (lane == 0 && chunk_bulk_ok<U, false>(src, nullptr, abs0 + (long long)chBeg * kWCH, a.n))
     chunk_bulk_issue<U, kIdx, false>(ws, 0, src, nullptr, abs0 + (long long)chBeg * kWCH);
@@ -472,7 +520,8 @@ __device__ __noinline__ void plan_item(const SortArgs& a, int level, int item,
   const int t0 = j * kThreads;
   if (tid < 7) sm.tot[tid] = __ldcg(&sdp->tot[tid]);
   if (j == 0 && tid == 0) {
-    segment_pivots<KT, U>(sdp, (const U*)(par ? a.keysB : a.keysA), level, (KT)a.flip, sm.piv);
+    segment_pivots<KT, U>(sdp, (const U*)(par ? a.keysB : a.keysA), level, (KT)a.flip, a.samples,
+                          sm.piv);
     sm.lut = pivot_lut(sm.piv[0] == sm.piv[1], sm.piv[1] == sm.piv[2]);
   }
   // counts of the segment's tiles before this item, and of this thread's tile
@@ -586,9 +635,9 @@ __device__ __noinline__ void plan_item(const SortArgs& a, int level, int item,
 // staged by class, and each class run written to base[class] + rank, where
 // base[class] starts at the tile's offset from the plan and advances by each
 // chunk's class counts: class runs of one chunk are contiguous and
-// consecutive chunks continue them.  Lanes 0..11 watch the children's pivot
-// positions a[start+n/2], a[start], a[stop] (lane 3*child + j) and copy the
-// staged key that lands there into the child's descriptor.
+// consecutive chunks continue them.  Lane 8*ci + j watches pivot samples j
+// and j + 8 of child ci (sample_pos) and copies the staged key that lands
+// there into the child's descriptor.
 template <typename U, bool kIdx>
 __device__ __forceinline__ void scatter_tile_warp(const SortArgs& a, int level, int t,
                                                   typename Persist<U, kIdx>::WarpArea& ws,
@@ -613,21 +662,20 @@ __device__ __forceinline__ void scatter_tile_warp(const SortArgs& a, int level, 
   const unsigned lut = __ldcg(&sdp->lut);
   // running destination of each class; pivot positions of the children
   if (lane < 7) ws.wbase[lane] = __ldcg(&a.tileOff[par][(long long)t * 8 + lane]);
+  const int ns = a.samples;
+  const int myci = lane >> 3, myj = lane & 7;
   bool watch = false;
-  if (lane < 12) {
-    const int ci = lane / 3, j = lane - 3 * (lane / 3);
-    const int child = __ldcg(&sdp->childSeg[ci]);
-    long long cpos = -1;
+  {
+    const int child = __ldcg(&sdp->childSeg[myci]);
     if (child >= 0) {
-      const long long cb = __ldcg(&sdp->cbase[2 * ci]);
-      const long long cn = __ldcg(&sdp->cbase[2 * ci + 1]) - cb;
-      cpos = j == 0 ? cb + cn / 2 : j == 1 ? cb : cb + cn - 1;
+      const long long cb = __ldcg(&sdp->cbase[2 * myci]);
+      const long long cn = __ldcg(&sdp->cbase[2 * myci + 1]) - cb;
+      if (myj < ns) ws.cpos[myci][myj] = sample_pos(cb, cn, myj, ns);
+      if (myj + 8 < ns) ws.cpos[myci][myj + 8] = sample_pos(cb, cn, myj + 8, ns);
+      watch = myj < ns;
     }
-    ws.cpos[lane] = cpos;
-    ws.cseg[lane] = child;
-    watch = child >= 0;
+    if (myj == 0) ws.cseg[myci] = child;
   }
-  watch = __any_sync(kFull, watch);
   __syncwarp();
 
   for (int ch = chBeg; ch < chEnd; ++ch) {
@@ -743,16 +791,21 @@ __device__ __forceinline__ void scatter_tile_warp(const SortArgs& a, int level, 
         }
       }
     }
-    // a child's pivot position written by this chunk: copy its key
-    if (watch && lane < 12) {
-      const int child = ws.cseg[lane];
-      if (child >= 0) {
-        const int ci = lane / 3;
-        const unsigned csA = ci == 0 ? 0u : ci == 1 ? cs2 : ci == 2 ? cs4 : cs6;
-        const unsigned csB = ci == 0 ? cs1 : ci == 1 ? cs3 : ci == 2 ? cs5 : nv;
-        const long long r = ws.cpos[lane] - ws.delta[2 * ci];
+    // a child's pivot sample written by this chunk: copy its key
+    if (watch) {
+      const unsigned csA = myci == 0 ? 0u : myci == 1 ? cs2 : myci == 2 ? cs4 : cs6;
+      const unsigned csB = myci == 0 ? cs1 : myci == 1 ? cs3 : myci == 2 ? cs5 : nv;
+      if (csB > csA) {
+        const int child = ws.cseg[myci];
+        const long long dl = ws.delta[2 * myci];
+        long long r = ws.cpos[myci][myj] - dl;
         if (r >= (long long)csA && r < (long long)csB)
-          a.segs[par ^ 1][child].piv[lane - 3 * ci] = (unsigned long long)ws.sk[r];
+          a.segs[par ^ 1][child].samp[myj] = (unsigned long long)ws.sk[r];
+        if (myj + 8 < ns) {
+          r = ws.cpos[myci][myj + 8] - dl;
+          if (r >= (long long)csA && r < (long long)csB)
+            a.segs[par ^ 1][child].samp[myj + 8] = (unsigned long long)ws.sk[r];
+        }
       }
     }
     __syncwarp();
