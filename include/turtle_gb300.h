@@ -197,13 +197,17 @@ turtle_status turtle_server_get_stats(turtle_server* srv, turtle_server_stats* o
 turtle_status turtle_server_destroy(turtle_server* srv);
 
 /* Pivot rule of this sorter (no counterpart in the reference; the output is
- * the same either way because every step is stable):
+ * the same whichever rule runs because every step is stable):
  *   TURTLE_PIVOTS_REFERENCE  sorted{a[start+n/2], a[start], a[stop]} per
  *                            segment, as the reference (turtle-sort.cu:641-655);
  *   TURTLE_PIVOTS_SAMPLED    the quartiles of 15 evenly spaced keys of the
- *                            segment (default): fewer partition levels. */
+ *                            segment (default): fewer partition levels;
+ *   TURTLE_PIVOTS_TWO_LEVEL  passes that apply two levels at once (31 classes;
+ *                            pivots from 63 evenly spaced keys): half the
+ *                            passes over the data, more work per key. */
 #define TURTLE_PIVOTS_REFERENCE 0
 #define TURTLE_PIVOTS_SAMPLED 1
+#define TURTLE_PIVOTS_TWO_LEVEL 2
 turtle_status turtle_set_pivot_rule(turtle_sorter* s, int rule);
 
 /* ---- introspection ---- */

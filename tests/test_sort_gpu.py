@@ -202,15 +202,16 @@ def test_errors():
 
 @pytest.mark.parametrize("dtype", [np.int32, np.uint8, np.int64, np.uint16])
 def test_pivot_rules_give_the_same_result(dtype):
-    """The reference pivot rule (median of start/middle/stop) and the sampled
-    rule (quartiles of 15 evenly spaced keys) must both produce the stable
-    order: pivots shape the partition tree, never the output."""
+    """The reference pivot rule (median of start/middle/stop), the sampled rule
+    (quartiles of 15 evenly spaced keys) and the two-level passes (31 classes
+    per pass) must all produce the stable order: pivots and pass shape form
+    the partition tree, never the output."""
     n = 700_001
     for dist, seed in [("uniform", 4), ("dups", 5), ("sorted", 6), ("organ", 7)]:
         k = make_keys(dtype, n, dist, seed)
         idx = np.arange(n, dtype=np.int32)
         outs = []
-        for rule in ("reference", "sampled"):
+        for rule in ("reference", "sampled", "two_level"):
             s = TurtleSort(dtype, n, track_index=True)
             s.set_pivot_rule(rule)
             ko, io = k.copy(), idx.copy()
@@ -219,4 +220,33 @@ def test_pivot_rules_give_the_same_result(dtype):
             s.close()
             check_sorted_pair(k, ko, io, idx)
             outs.append((ko, io))
-        assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+        for o in outs[1:]:
+            assert np.array_equal(outs[0][0], o[0]) and np.array_equal(outs[0][1], o[1])
+
+
+_TWO_LEVEL: dict = {}
+
+
+@pytest.mark.parametrize("dtype", ALL_DTYPES)
+@pytest.mark.parametrize("dist", ["uniform", "dups", "equal", "sorted", "reverse", "organ",
+                                  "extremes", "two"])
+def test_two_level_passes(dtype, dist):
+    """Two-level passes: every dtype and key distribution, sizes from one tile
+    to several passes deep, with and without ids."""
+    key = np.dtype(dtype)
+    if key not in _TWO_LEVEL:
+        _TWO_LEVEL[key] = TurtleSort(dtype, 1 << 21, track_index=True)
+        _TWO_LEVEL[key].set_pivot_rule("two_level")
+    s = _TWO_LEVEL[key]
+    t = tile(dtype)
+    for n in [t + 1, 4 * t + 7, 70_001, 1 << 21]:
+        k = make_keys(dtype, n, dist, n % 97)
+        idx = np.arange(n, dtype=np.int32)
+        ko, io = k.copy(), idx.copy()
+        s.StartSorting(ko, io)
+        s.Sync()
+        check_sorted_pair(k, ko, io, idx)
+        ko = k.copy()
+        s.StartSorting(ko)
+        s.Sync()
+        assert np.array_equal(ko, np.sort(k, kind="stable"))

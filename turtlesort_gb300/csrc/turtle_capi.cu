@@ -408,7 +408,7 @@ turtle_status turtle_sort_batched_device(turtle_sorter* s, void* d_keys, int32_t
   cudaStream_t cs = pick_stream(s, stream);
   std::lock_guard<std::mutex> lk(s->mu);
   // every small array may become one leaf at once
-  if ((long long)s->lay.leafCap < num + 8LL * (s->lay.segCap + 1) + 4096) {
+  if ((long long)s->lay.leafCap < num + 16LL * (s->lay.segCap + 1) + 4096) {
     TRY_CUDA(s, cudaDeviceSynchronize());
     free_graphs(s);
     if ((st = alloc_workspace(s, num)) != TURTLE_OK) return st;
@@ -510,7 +510,7 @@ int turtle_debug_timeline(const turtle_sorter* s, uint64_t* ns, int32_t* info, i
 }
 
 turtle_status turtle_set_pivot_rule(turtle_sorter* s, int rule) {
-  if (!s || (rule != turtle::kRuleReference && rule != turtle::kRuleSampled))
+  if (!s || rule < turtle::kRuleReference || rule > turtle::kRuleTwoLevel)
     return TURTLE_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lk(s->mu);
   free_graphs(s);  // captured launches hold the old rule

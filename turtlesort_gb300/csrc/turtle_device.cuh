@@ -14,6 +14,7 @@
 #pragma once
 
 #include <cuda/atomic>
+#include <climits>
 #include <cstdint>
 #include <type_traits>
 
@@ -41,7 +42,9 @@ constexpr int kFillChunk = 1 << 16;      // pivot-run fill work unit (elements)
 constexpr int kDepthSwitch = TURTLE_DEPTH_SWITCH;  // levels of start/mid/stop pivots
                                          // before switching to sampled quartile pivots
 constexpr int kMaxLevels = 4096;         // hard cap on partition levels
-constexpr int kSamples = 15;             // evenly spaced pivot samples (sampled rule)
+constexpr int kSamples = 15;             // evenly spaced pivot samples (one-level sampled rule)
+constexpr int kWideSamples = 63;         // pivot samples of a segment in two-level passes
+constexpr int kRow = 32;                 // per-tile row: 32 class counts / offsets / sample keys
 constexpr int kLeafClasses = 10;         // group sizes 1, 2, 4, ..., 512 threads
 constexpr long long kSpinLimit = 40000000LL;  // bounded barrier spin iterations
 constexpr int kTimeline = 160;           // phase timestamps kept per launch
@@ -92,18 +95,32 @@ struct SegDesc {        // a segment partitioned by the multi-CTA 3-pivot pass
   long long n;
   int tileBase;         // first entry in this level's tile arrays
   int ntiles;
-  unsigned long long samp[16]; // pivot samples (unsigned images; captured by the
-                               // parent's scatter): a[start+n/2], a[start], a[stop]
-                               // under the reference rule, else kSamples evenly
-                               // spaced keys
-  unsigned long long pivS[3];  // sorted pivots (unsigned images), set by the plan
+  unsigned long long samp[64]; // pivot samples (unsigned images): a[start+n/2], a[start],
+                               // a[stop] under the reference rule, else evenly spaced
+                               // keys (one-level) or up to kWideSamples keys (two-level)
+  int nsamp;            // valid entries of samp (two-level passes)
   unsigned lut;         // class remap for equal pivots, set by the plan
-  int pad;
-  long long cbase[8];   // class boundaries after planning (cbase[7] = end)
-  int childSeg[4];      // next-level segment of classes 0,2,4,6 (-1: none)
-  int tot[8];           // class totals, summed by COUNT
+  unsigned long long pivS[3];  // sorted pivots (unsigned images), set by the plan
+  unsigned long long cpiv[4][3];  // two-level: sorted pivots of the children (classes 0,2,4,6)
+  unsigned clut[4];     // two-level: their class tables
+  long long cbase[32];  // class boundaries after planning (one-level: 8, two-level: 32)
+  int childSeg[16];     // next-level segments (one-level: 4 children, two-level: 16 grandchildren)
+  int tot[32];          // class totals, summed by COUNT
   int planBase;         // first plan item of this segment
-  int pad2;
+  unsigned parkMask;    // two-level: classes whose keys wait in B for a fill
+};
+// Sorted pivots and class table of one 3-pivot split (16 bytes for 32-bit
+// keys: one shared-memory load).
+template <typename KT>
+struct alignas(16) PivotSet {
+  KT p[3];
+  unsigned lut;
+};
+// Pivots of a segment and of its four children (two-level passes).
+template <typename KT>
+struct WidePivots {
+  PivotSet<KT> par;       // the segment's pivots
+  PivotSet<KT> child[4];  // child ci's (parent classes 0, 2, 4, 6)
 };
 struct TileDesc {       // one partition tile: [lo, hi) of segment seg
   long long lo;
@@ -165,16 +182,17 @@ struct SortArgs {
   unsigned long long flip;   // sign-bit mask for signed dtypes (0 otherwise)
   SegDesc* segs[2];
   TileDesc* tiles[2];
-  int* tileCnt[2];           // [tile][8]: #(k<p1), #(k<=p1), #(k<p2), #(k<=p2), #(k<p3),
-                             // #(k<=p3), #keys (predicate totals against the segment's pivots)
-  long long* tileOff[2];     // [tile][8] global destination of each class
+  int* tileCnt[2];           // [tile][kRow]: one-level: #(k<p1), #(k<=p1), #(k<p2), #(k<=p2),
+                             // #(k<p3), #(k<=p3), #keys; two-level: the 31 class counts
+  long long* tileOff[2];     // [tile][kRow] global destination of each class
   int* planSeg[2];           // segment of each plan item (kPartTile * kThreads keys)
   LeafDesc* leaves;
   LeafDesc* leavesSorted;
   FillDesc* fills;
   int segCap, tileCap, leafCap, fillCap, planCap;
   int resume;                // 1: continue a partition that yielded
-  int samples;               // pivot samples per segment: 3 (reference rule) or kSamples
+  int samples;               // pivot samples per segment: 3 (reference rule, one-level
+                             // passes) or kWideSamples (sampled rule, two-level passes)
   Control* ctrl;
 };
 

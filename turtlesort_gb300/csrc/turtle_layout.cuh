@@ -27,8 +27,9 @@ inline WsLayout make_layout(long long maxN, int tile, int leafMax, long long ext
   const long long tileCap = maxN / tile + 2 * segCap + 64;
   // leaf / fill lists: roomy enough that a partition never has to yield on
   // ordinary inputs (one level adds at most 4 leaves and 3 fills per segment)
-  const long long leafCap = std::max(8 * (segCap + 1), maxN / 64) + extraLeaves + 4096;
-  const long long fillCap = 2 * (3 * (segCap + 1) + tileCap) + maxN / 64 + 4096;
+  // (a two-level pass adds up to 16 leaves and 15 fills per segment)
+  const long long leafCap = std::max(24 * (segCap + 1), maxN / 64) + extraLeaves + 4096;
+  const long long fillCap = 2 * (15 * (segCap + 1) + tileCap) + maxN / 64 + 4096;
   // plan items: kThreads tiles each, at least one per segment
   const long long planCap = tileCap / turtle::kThreads + segCap + 64;
   L.planCap = (int)planCap;
@@ -40,8 +41,8 @@ inline WsLayout make_layout(long long maxN, int tile, int leafMax, long long ext
   L.offCtrl = o; o = align_up(o + sizeof(turtle::Control), 256);
   for (int p = 0; p < 2; ++p) { L.offSegs[p] = o; o = align_up(o + segCap * sizeof(turtle::SegDesc), 256); }
   for (int p = 0; p < 2; ++p) { L.offTiles[p] = o; o = align_up(o + tileCap * sizeof(turtle::TileDesc), 256); }
-  for (int p = 0; p < 2; ++p) { L.offTileCnt[p] = o; o = align_up(o + tileCap * 8 * sizeof(int), 256); }
-  for (int p = 0; p < 2; ++p) { L.offTileOff[p] = o; o = align_up(o + tileCap * 8 * sizeof(long long), 256); }
+  for (int p = 0; p < 2; ++p) { L.offTileCnt[p] = o; o = align_up(o + tileCap * turtle::kRow * sizeof(int), 256); }
+  for (int p = 0; p < 2; ++p) { L.offTileOff[p] = o; o = align_up(o + tileCap * turtle::kRow * sizeof(long long), 256); }
   for (int p = 0; p < 2; ++p) { L.offPlanSeg[p] = o; o = align_up(o + planCap * sizeof(int), 256); }
   L.offLeaves = o; o = align_up(o + leafCap * sizeof(turtle::LeafDesc), 256);
   L.offLeavesSorted = o; o = align_up(o + leafCap * sizeof(turtle::LeafDesc), 256);
@@ -73,11 +74,15 @@ inline unsigned long long dtype_flip(int dt) {
 // Kernel arguments for sorting `keys` (+ `idx`) with scratch buffers
 // keysB / idxB and the work lists laid out by L inside `ws`.
 // Pivot rules: the reference's median of a[start+n/2], a[start], a[stop]
-// (3 samples) or the quartiles of kSamples evenly spaced samples.  Both give
-// the same output (every step is stable); the sampled rule needs fewer levels.
+// (3 samples), the quartiles of kSamples evenly spaced samples, or two-level
+// passes with kWideSamples samples.  All give the same output (every step is
+// stable); the sampled rules need fewer levels.
 constexpr int kRuleReference = 0;
 constexpr int kRuleSampled = 1;
-inline int rule_samples(int rule) { return rule == kRuleReference ? 3 : kSamples; }
+constexpr int kRuleTwoLevel = 2;
+inline int rule_samples(int rule) {
+  return rule == kRuleReference ? 3 : rule == kRuleTwoLevel ? kWideSamples : kSamples;
+}
 
 inline SortArgs bind_args(void* keys, int* idx, void* keysB, int* idxB, char* ws, const WsLayout& L,
                           const long long* offs, long long num, long long n,

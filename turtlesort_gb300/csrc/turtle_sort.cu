@@ -78,10 +78,25 @@ struct Persist {
     KT sk[kWCH];                    // staged keys (class order)
     int si[kIdx ? kWCH : 4];        // staged ids
     unsigned char sc[kWCH];         // class of each stage slot
-    long long delta[8];             // destination minus stage slot, per class
-    long long wbase[8];             // running destination per class
-    long long cpos[4][16];          // children's pivot sample positions
-    int cseg[4];                    // the child segments (-1: none)
+    struct OneLevel {               // tables of a one-level pass (7 classes)
+      long long delta[8];           // destination minus stage slot, per class
+      long long wbase[8];           // running destination per class
+      long long cpos[4][16];        // children's pivot sample positions
+      int cseg[4];                  // the child segments (-1: none)
+    };
+    struct TwoLevel {               // tables of a two-level pass (31 classes)
+      long long delta[32];          // destination minus stage slot, per class
+      long long wbase[32];          // running destination per class
+      long long capP[32];           // next sample position of each grandchild class
+      unsigned bword[8][32];        // per lane: stage slot of its first key of each class
+      int capI[32];                 // index of that sample
+      WidePivots<KT> wp;            // pivots of segment pivSeg
+      int pivSeg;
+    };
+    union {
+      OneLevel o;
+      TwoLevel t;
+    };
     unsigned long long mbar[2];     // bulk-copy completion barriers
   };
 
@@ -99,6 +114,11 @@ struct Persist {
     unsigned lut;
     int classOff[16];
     int classItems[16];
+    // two-level plan
+    int wcb[33];                    // class starts relative to the segment
+    int gSeg[16], gTb[16], gNt[16]; // the grandchild segments
+    long long gStart[16], gN[16];
+    WidePivots<KT> wpiv;
   };
 
   static constexpr int kLIdxSlots = kIdx ? G::kLeafIdxSlots : 4;
@@ -238,12 +258,13 @@ __device__ int alloc_segment(const SortArgs& a, int par, long long start, long l
   }
   SegDesc d;
   d.start = start; d.n = n; d.tileBase = (int)tb; d.ntiles = (int)nt;
-  for (int i = 0; i < 16; ++i) d.samp[i] = 0;
+  d.nsamp = 0;
   d.pivS[0] = d.pivS[1] = d.pivS[2] = 0;
-  d.lut = 0; d.pad = 0;
-  for (int c = 0; c < 8; ++c) { d.cbase[c] = 0; d.tot[c] = 0; }
-  for (int c = 0; c < 4; ++c) d.childSeg[c] = -1;
-  d.planBase = pb; d.pad2 = 0;
+  d.lut = 0;
+  for (int c = 0; c < 32; ++c) { d.cbase[c] = 0; d.tot[c] = 0; }
+  for (int c = 0; c < 16; ++c) d.childSeg[c] = -1;
+  d.planBase = pb;
+  d.parkMask = 0u;
   a.segs[par][si] = d;
   for (int k = 0; k < np; ++k) a.planSeg[par][pb + k] = si;
   *tbOut = (int)tb;
@@ -316,6 +337,7 @@ __device__ void route_input(const SortArgs& a, long long start, long long n, boo
   const U* src = (const U*)a.keysA;
   const KT flip = (KT)a.flip;
   SegDesc* sd = &a.segs[0][si];
+  sd->nsamp = a.samples;
   for (int i = 0; i < a.samples; ++i)
     sd->samp[i] = (unsigned long long)kload<U, KT>(src, sample_pos(start, n, i, a.samples), flip);
   if (writeTiles) write_tiles<kTile>(a, 0, si, tb, nt, start, n, 0, 1);
@@ -469,7 +491,7 @@ __device__ __forceinline__ void count_tile_warp(const SortArgs& a, int level, in
     int v = (lane & 1) ? (int)(w >> 16) : (int)(w & 0xffffu);
     if (lane == 6) v = rhi - rlo;
     if (lane == 7) v = 0;
-    a.tileCnt[par][(long long)t * 8 + lane] = v;
+    a.tileCnt[par][(long long)t * kRow + lane] = v;
   }
   // the tile's class counts go to the warp's running total of its segment
   {
@@ -516,7 +538,7 @@ __device__ __noinline__ void plan_item(const SortArgs& a, int level, int item,
   const long long sdStart = __ldcg(&sdp->start);
   const int tileBase = __ldcg(&sdp->tileBase);
   const int nt = __ldcg(&sdp->ntiles);
-  const int* cnt = a.tileCnt[par] + (long long)tileBase * 8;
+  const int* cnt = a.tileCnt[par] + (long long)tileBase * kRow;
   const int t0 = j * kThreads;
   if (tid < 7) sm.tot[tid] = __ldcg(&sdp->tot[tid]);
   if (j == 0 && tid == 0) {
@@ -530,12 +552,12 @@ __device__ __noinline__ void plan_item(const SortArgs& a, int level, int item,
   for (int c = 0; c < 7; ++c) { pre[c] = 0; v[c] = 0; }
   for (int t = tid; t < t0; t += kThreads) {
     int w[7];
-    tile_classes(cnt + (long long)t * 8, w);
+    tile_classes(cnt + (long long)t * kRow, w);
 #pragma unroll
     for (int c = 0; c < 7; ++c) pre[c] += w[c];
   }
   const int myTile = t0 + tid;
-  if (myTile < nt) tile_classes(cnt + (long long)myTile * 8, v);
+  if (myTile < nt) tile_classes(cnt + (long long)myTile * kRow, v);
   int inc[7];
 #pragma unroll
   for (int c = 0; c < 7; ++c) {
@@ -571,7 +593,7 @@ __device__ __noinline__ void plan_item(const SortArgs& a, int level, int item,
 #pragma unroll
     for (int c = 0; c < 7; ++c)
       o[c] = sdStart + sm.cbase[c] + sm.pre[c] + sm.red[warp][c] + (inc[c] - v[c]);
-    longlong2* dst = reinterpret_cast<longlong2*>(a.tileOff[par] + (long long)(tileBase + myTile) * 8);
+    longlong2* dst = reinterpret_cast<longlong2*>(a.tileOff[par] + (long long)(tileBase + myTile) * kRow);
     dst[0] = make_longlong2(o[0], o[1]);
     dst[1] = make_longlong2(o[2], o[3]);
     dst[2] = make_longlong2(o[4], o[5]);
@@ -661,7 +683,7 @@ __device__ __forceinline__ void scatter_tile_warp(const SortArgs& a, int level, 
            p3 = (KT)__ldcg(&sdp->pivS[2]);
   const unsigned lut = __ldcg(&sdp->lut);
   // running destination of each class; pivot positions of the children
-  if (lane < 7) ws.wbase[lane] = __ldcg(&a.tileOff[par][(long long)t * 8 + lane]);
+  if (lane < 7) ws.o.wbase[lane] = __ldcg(&a.tileOff[par][(long long)t * kRow + lane]);
   const int ns = a.samples;
   const int myci = lane >> 3, myj = lane & 7;
   bool watch = false;
@@ -670,11 +692,11 @@ __device__ __forceinline__ void scatter_tile_warp(const SortArgs& a, int level, 
     if (child >= 0) {
       const long long cb = __ldcg(&sdp->cbase[2 * myci]);
       const long long cn = __ldcg(&sdp->cbase[2 * myci + 1]) - cb;
-      if (myj < ns) ws.cpos[myci][myj] = sample_pos(cb, cn, myj, ns);
-      if (myj + 8 < ns) ws.cpos[myci][myj + 8] = sample_pos(cb, cn, myj + 8, ns);
+      if (myj < ns) ws.o.cpos[myci][myj] = sample_pos(cb, cn, myj, ns);
+      if (myj + 8 < ns) ws.o.cpos[myci][myj + 8] = sample_pos(cb, cn, myj + 8, ns);
       watch = myj < ns;
     }
-    if (myj == 0) ws.cseg[myci] = child;
+    if (myj == 0) ws.o.cseg[myci] = child;
   }
   __syncwarp();
 
@@ -770,9 +792,9 @@ __device__ __forceinline__ void scatter_tile_warp(const SortArgs& a, int level, 
                          : lane == 5 ? cs5 : lane == 6 ? cs6 : 0u;
       const unsigned cel = lane == 0 ? cs1 : lane == 1 ? cs2 : lane == 2 ? cs3 : lane == 3 ? cs4
                          : lane == 4 ? cs5 : lane == 5 ? cs6 : nv;
-      const long long wb = ws.wbase[lane];
-      ws.delta[lane] = wb - (long long)csl;
-      ws.wbase[lane] = wb + (long long)(cel - csl);
+      const long long wb = ws.o.wbase[lane];
+      ws.o.delta[lane] = wb - (long long)csl;
+      ws.o.wbase[lane] = wb + (long long)(cel - csl);
     }
     __syncwarp();
     // write-out: consecutive stage slots of one class go to consecutive addresses
@@ -785,7 +807,7 @@ __device__ __forceinline__ void scatter_tile_warp(const SortArgs& a, int level, 
         const int sl = 32 * j + lane;
         if (sl < (int)nv) {
           const unsigned c = ws.sc[sl];
-          const long long d = ws.delta[c] + sl;
+          const long long d = ws.o.delta[c] + sl;
           if (!(parkPivots && (c & 1u))) dstK[d] = U(ws.sk[sl] ^ flip);
           if (kIdx) dstI[d] = ws.si[sl];
         }
@@ -796,13 +818,13 @@ __device__ __forceinline__ void scatter_tile_warp(const SortArgs& a, int level, 
       const unsigned csA = myci == 0 ? 0u : myci == 1 ? cs2 : myci == 2 ? cs4 : cs6;
       const unsigned csB = myci == 0 ? cs1 : myci == 1 ? cs3 : myci == 2 ? cs5 : nv;
       if (csB > csA) {
-        const int child = ws.cseg[myci];
-        const long long dl = ws.delta[2 * myci];
-        long long r = ws.cpos[myci][myj] - dl;
+        const int child = ws.o.cseg[myci];
+        const long long dl = ws.o.delta[2 * myci];
+        long long r = ws.o.cpos[myci][myj] - dl;
         if (r >= (long long)csA && r < (long long)csB)
           a.segs[par ^ 1][child].samp[myj] = (unsigned long long)ws.sk[r];
         if (myj + 8 < ns) {
-          r = ws.cpos[myci][myj + 8] - dl;
+          r = ws.o.cpos[myci][myj + 8] - dl;
           if (r >= (long long)csA && r < (long long)csB)
             a.segs[par ^ 1][child].samp[myj + 8] = (unsigned long long)ws.sk[r];
         }
@@ -811,6 +833,12 @@ __device__ __forceinline__ void scatter_tile_warp(const SortArgs& a, int level, 
     __syncwarp();
   }
 }
+
+}  // namespace turtle
+
+#include "turtle_wide.cuh"
+
+namespace turtle {
 
 // ---------------------------------------------------------------------------
 // leaf bucketing (end of the partition kernel)
@@ -875,7 +903,8 @@ __device__ __noinline__ bool leaf_bucket(const SortArgs& a, typename Persist<U, 
 
 // Tiles of a level, claimed one at a time by each warp (lane 0 claims the
 // next tile before the warp works on the current one).
-template <typename U, bool kIdx, int kPhase>
+// kWide: two-level pass (31 classes) instead of one level (7 classes).
+template <typename U, bool kIdx, int kPhase, bool kWide>
 __device__ __forceinline__ void stream_tiles(const SortArgs& a, int level, int ntiles,
                                              unsigned* wc,
                                              typename Persist<U, kIdx>::WarpArea& ws,
@@ -884,6 +913,8 @@ __device__ __forceinline__ void stream_tiles(const SortArgs& a, int level, int n
   // the bulk copies of this phase read what other CTAs wrote before the
   // grid barrier: order the async proxy after it
   if (lane == 0) fence_proxy_async();
+  if (kWide) ws.t.pivSeg = -1;  // segment indices are per pass
+  __syncwarp();
   unsigned t = 0;
   if (lane == 0) t = atomicAdd(wc, 1u);
   t = __shfl_sync(kFull, t, 0);
@@ -891,15 +922,22 @@ __device__ __forceinline__ void stream_tiles(const SortArgs& a, int level, int n
   while ((int)t < ntiles) {
     unsigned nxt = 0;
     if (lane == 0) nxt = atomicAdd(wc, 1u);
-    if (kPhase == 0) count_tile_warp<U, kIdx>(a, level, (int)t, ws, mphase, accSeg, accCnt);
-    else scatter_tile_warp<U, kIdx>(a, level, (int)t, ws, mphase);
+    if (kWide) {
+      if (kPhase == 0) count31_tile_warp<U, kIdx>(a, level, (int)t, ws, mphase, accSeg, accCnt);
+      else scatter31_tile_warp<U, kIdx>(a, level, (int)t, ws, mphase);
+    } else {
+      if (kPhase == 0) count_tile_warp<U, kIdx>(a, level, (int)t, ws, mphase, accSeg, accCnt);
+      else scatter_tile_warp<U, kIdx>(a, level, (int)t, ws, mphase);
+    }
     t = __shfl_sync(kFull, nxt, 0);
   }
-  if (kPhase == 0 && accSeg >= 0 && lane < 7 && accCnt)
+  if (kPhase == 0 && accSeg >= 0 && lane < (kWide ? 32 : 7) && accCnt)
     atomicAdd(&a.segs[level & 1][accSeg].tot[lane], accCnt);
 }
 
-template <typename U, bool kIdx>
+// kWide: two-level passes (sampled pivots from kWideSamples keys) instead of
+// one level per pass; each form is its own kernel with its own registers.
+template <typename U, bool kIdx, bool kWide>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(SortArgs a) {
   using P = Persist<U, kIdx>;
   constexpr int kTile = P::kTile, kLeafMax = P::kLeafMax;
@@ -953,10 +991,12 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
   if (!grid_barrier(c)) return;
   timeline_mark(c, 0);
 
-  // one level adds at most 4 leaves and 3 fills (+ chunks) per segment; stop
-  // and hand the lists to leaf_kernel before a level could overflow them
-  const int leafRoom = 4 * (a.segCap + 1);
-  const int fillRoom = 3 * (a.segCap + 1) + a.tileCap;
+  // one level adds at most 4 leaves and 3 fills (+ chunks) per segment, a
+  // two-level pass 16 leaves and 15 fills; stop and hand the lists to
+  // leaf_kernel before a level could overflow them
+  constexpr bool wide = kWide;
+  const int leafRoom = (wide ? 16 : 4) * (a.segCap + 1);
+  const int fillRoom = (wide ? 15 : 3) * (a.segCap + 1) + a.tileCap;
   for (;; ++level) {
     const int par = level & 1;
     cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> st(c->segTile[par]);
@@ -978,7 +1018,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
 
     // COUNT: per-tile predicate totals
     if (blockIdx.x == 0 && tid == 0) c->work[(phase + 2) & 3] = 0;
-    stream_tiles<U, kIdx, 0>(a, level, ntiles, &c->work[phase & 3], ws, mphase);
+    stream_tiles<U, kIdx, 0, kWide>(a, level, ntiles, &c->work[phase & 3], ws, mphase);
     ++phase;
     __threadfence();
     if (!grid_barrier(c)) return;
@@ -991,7 +1031,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
       for (;;) {
         const int it = claim_item(wc);
         if (it >= nplan) break;
-        plan_item<U, kIdx>(a, level, it, sm);
+        if (kWide) plan31_item<U, kIdx>(a, level, it, sm);
+        else plan_item<U, kIdx>(a, level, it, sm);
       }
       ++phase;
     }
@@ -1007,13 +1048,13 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
       c->planCount[par] = 0;
       c->work[(phase + 2) & 3] = 0;
     }
-    stream_tiles<U, kIdx, 1>(a, level, ntiles, &c->work[phase & 3], ws, mphase);
+    stream_tiles<U, kIdx, 1, kWide>(a, level, ntiles, &c->work[phase & 3], ws, mphase);
     ++phase;
     __threadfence();
     if (!grid_barrier(c)) return;
     timeline_mark(c, nsegs);
   }
-  if (blockIdx.x == 0 && tid == 0) c->levels = level;
+  if (blockIdx.x == 0 && tid == 0) c->levels = wide ? 2 * level : level;
   // publish the leaves for leaf_kernel (launched right after on the stream)
   leaf_bucket<U, kIdx>(a, sm);
 }
@@ -1178,8 +1219,11 @@ template <typename U, bool kIdx>
 static cudaError_t prepare_persistent(int device, int* gridOut) {
   const size_t smem = persist_smem_bytes<U, kIdx>();
   const size_t lsmem = leaf_smem_bytes<U, kIdx>();
-  cudaError_t e = cudaFuncSetAttribute(persistent_sort_kernel<U, kIdx>,
+  cudaError_t e = cudaFuncSetAttribute(persistent_sort_kernel<U, kIdx, false>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(persistent_sort_kernel<U, kIdx, true>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(multisort_kernel<U, kIdx>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)lsmem);
@@ -1187,10 +1231,15 @@ static cudaError_t prepare_persistent(int device, int* gridOut) {
   e = cudaFuncSetAttribute(leaf_kernel<U, kIdx>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)lsmem);
   if (e != cudaSuccess) return e;
-  int perSM = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, persistent_sort_kernel<U, kIdx>,
+  int perSM = 0, perSMWide = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, persistent_sort_kernel<U, kIdx, false>,
                                                     kThreads, smem);
   if (e != cudaSuccess) return e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSMWide,
+                                                    persistent_sort_kernel<U, kIdx, true>, kThreads,
+                                                    smem);
+  if (e != cudaSuccess) return e;
+  perSM = perSM < perSMWide ? perSM : perSMWide;  // one grid serves both forms
   int sms = 0;
   e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   if (e != cudaSuccess) return e;
@@ -1212,7 +1261,9 @@ static cudaError_t launch_persistent(const SortArgs& a, int grid, cudaStream_t s
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  cudaError_t e = cudaLaunchKernelEx(&cfg, persistent_sort_kernel<U, kIdx>, a);
+  cudaError_t e = a.samples == kWideSamples
+                      ? cudaLaunchKernelEx(&cfg, persistent_sort_kernel<U, kIdx, true>, a)
+                      : cudaLaunchKernelEx(&cfg, persistent_sort_kernel<U, kIdx, false>, a);
   if (e != cudaSuccess) return e;
   if (mid != nullptr && (e = cudaEventRecord(mid, stream)) != cudaSuccess) return e;
   int sms = 0, dev = 0;

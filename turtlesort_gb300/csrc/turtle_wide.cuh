@@ -1,0 +1,577 @@
+// Two-level partition passes of persistent_sort_kernel (sampled pivot rule).
+//
+// One pass applies two levels of the 3-pivot partition at once.  Every key is
+// classified by its segment's pivots (class c1 of 7) and, when c1 is not a
+// pivot run, by the pivots of child c1/2 (class c2 of 7).  The 31 classes
+// k = 8*(c1/2) + (c1 odd ? 7 : c2) are in key order, so one stable counting
+// pass (COUNT, PLAN, SCATTER as in the one-level pass) moves every key
+// straight to its grandchild: half the passes over the data, half the grid
+// barriers.  A segment's pivots are the quartiles of its kWideSamples evenly
+// spaced samples; child ci's pivots are the quartiles of the samples that fall
+// in child ci.  SCATTER records the samples of every new grandchild segment
+// as it writes the keys at the sample positions.  Every step is stable, so the
+// output is the stable sort by key whatever the samples are.
+#pragma once
+
+namespace turtle {
+
+constexpr int kWideClasses = 31;  // classes of a two-level pass (class 31 unused)
+
+__device__ __forceinline__ unsigned wide_class(unsigned c1, unsigned c2) {
+  return (c1 >> 1) * 8u + ((c1 & 1u) ? 7u : c2);
+}
+
+// Position of sample i of ns in a segment of m keys starting at pos.
+__device__ __forceinline__ long long wide_sample_pos(long long pos, long long m, int i, int ns) {
+  return pos + ((2 * (long long)i + 1) * m) / (2 * ns);
+}
+
+// The pivots of a segment and of its four children from its samples, by one
+// warp (every caller gets the same result).  The samples (two per lane) are
+// sorted by a bitonic network; the parent pivots are ranks ns/4, ns/2, 3ns/4.
+// The samples of parent class 2ci are contiguous in the sorted order; child
+// ci's pivots are their quartiles, or the neighbouring parent pivots when the
+// class holds no sample.
+template <typename KT>
+__device__ __noinline__ void wide_pivots_warp(const SegDesc* sd, WidePivots<KT>* out) {
+  const int lane = threadIdx.x & 31;
+  const int ns = __ldcg(&sd->nsamp);
+  const int e0 = 2 * lane, e1 = 2 * lane + 1;
+  KT x0 = e0 < ns ? (KT)__ldcg(&sd->samp[e0]) : key_max<KT>();
+  KT x1 = e1 < ns ? (KT)__ldcg(&sd->samp[e1]) : key_max<KT>();
+#pragma unroll
+  for (int k = 2; k <= 64; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      if (j == 1) {
+        const bool asc = (e0 & k) == 0;
+        const KT lo = x0 < x1 ? x0 : x1, hi = x0 < x1 ? x1 : x0;
+        x0 = asc ? lo : hi;
+        x1 = asc ? hi : lo;
+      } else {
+        const KT y0 = __shfl_xor_sync(0xffffffffu, x0, j >> 1);
+        const KT y1 = __shfl_xor_sync(0xffffffffu, x1, j >> 1);
+        const bool keepMin0 = ((e0 & k) == 0) == ((e0 & j) == 0);
+        const bool keepMin1 = ((e1 & k) == 0) == ((e1 & j) == 0);
+        x0 = keepMin0 ? (y0 < x0 ? y0 : x0) : (y0 < x0 ? x0 : y0);
+        x1 = keepMin1 ? (y1 < x1 ? y1 : x1) : (y1 < x1 ? x1 : y1);
+      }
+    }
+  }
+  // sorted sample of rank r (warp-uniform r)
+  auto at = [&](int r) -> KT {
+    return __shfl_sync(0xffffffffu, (r & 1) ? x1 : x0, (r >> 1) & 31);
+  };
+  WidePivots<KT> wp;
+  PivotSet<KT>& pp = wp.par;
+  pp.p[0] = at(ns / 4);
+  pp.p[1] = at(ns / 2);
+  pp.p[2] = at((3 * ns) / 4);
+  pp.lut = pivot_lut(pp.p[0] == pp.p[1], pp.p[1] == pp.p[2]);
+  const int c0 = e0 < ns ? class_lut<KT>(x0, pp.p[0], pp.p[1], pp.p[2], pp.lut) : 99;
+  const int c1 = e1 < ns ? class_lut<KT>(x1, pp.p[0], pp.p[1], pp.p[2], pp.lut) : 99;
+#pragma unroll
+  for (int ci = 0; ci < 4; ++ci) {
+    const int want = 2 * ci;
+    const int below = __popc(__ballot_sync(0xffffffffu, c0 < want)) +
+                      __popc(__ballot_sync(0xffffffffu, c1 < want));
+    const int cnt = __popc(__ballot_sync(0xffffffffu, c0 == want)) +
+                    __popc(__ballot_sync(0xffffffffu, c1 == want));
+    PivotSet<KT>& cs = wp.child[ci];
+    if (cnt > 0) {
+      cs.p[0] = at(below + cnt / 4);
+      cs.p[1] = at(below + cnt / 2);
+      cs.p[2] = at(below + (3 * cnt) / 4);
+    } else {
+      const KT lo = ci == 0 ? pp.p[0] : pp.p[ci - 1];
+      const KT hi = ci == 3 ? pp.p[2] : pp.p[ci];
+      cs.p[0] = lo;
+      cs.p[1] = lo;
+      cs.p[2] = hi;
+    }
+    cs.lut = pivot_lut(cs.p[0] == cs.p[1], cs.p[1] == cs.p[2]);
+  }
+  if (lane == 0) *out = wp;
+  __syncwarp();
+}
+
+// Class (0..30) of key k: the parent's pivots in registers, the children's
+// in shared memory (one load of the child's set per key).
+template <typename KT>
+__device__ __forceinline__ unsigned wide_class_of(KT k, const PivotSet<KT>& pp,
+                                                  const PivotSet<KT>* child) {
+  const unsigned c1 = (unsigned)class_lut<KT>(k, pp.p[0], pp.p[1], pp.p[2], pp.lut);
+  const PivotSet<KT> cs = child[(c1 >> 1) & 3u];
+  const unsigned c2 = (unsigned)class_lut<KT>(k, cs.p[0], cs.p[1], cs.p[2], cs.lut);
+  return wide_class(c1, c2);
+}
+
+// Lane counts of one chunk: 4-bit fields, word w = classes 8w..8w+7.
+__device__ __forceinline__ void wide_bump(unsigned* acc4, unsigned k) {
+  const unsigned w = k >> 3, inc = 1u << (4u * (k & 7u));
+  acc4[0] += w == 0u ? inc : 0u;
+  acc4[1] += w == 1u ? inc : 0u;
+  acc4[2] += w == 2u ? inc : 0u;
+  acc4[3] += w == 3u ? inc : 0u;
+}
+
+// Widen a word of eight 4-bit fields to two words of four 8-bit fields.
+__device__ __forceinline__ unsigned widen_lo(unsigned x) {
+  return (x & 0xFu) | ((x & 0xF0u) << 4) | ((x & 0xF00u) << 8) | ((x & 0xF000u) << 12);
+}
+__device__ __forceinline__ unsigned widen_hi(unsigned x) {
+  return ((x >> 16) & 0xFu) | ((x >> 12) & 0xF00u) | ((x >> 8) & 0xF0000u) |
+         ((x >> 4) & 0xF000000u);
+}
+
+// Warp totals of eight words of four 8-bit fields (classes 4w..4w+3): lane k
+// returns the total of class k.  One reduction per two classes (16-bit sums).
+__device__ __forceinline__ int wide_totals(const unsigned* a8) {
+  const int lane = threadIdx.x & 31;
+  int mine = 0;
+#pragma unroll
+  for (int w = 0; w < 8; ++w) {
+    const unsigned x = a8[w];
+    const unsigned lo = __reduce_add_sync(0xffffffffu, (x & 0xFFu) | ((x & 0xFF00u) << 8));
+    const unsigned hi = __reduce_add_sync(0xffffffffu, ((x >> 16) & 0xFFu) | ((x >> 8) & 0xFF0000u));
+    const int k0 = 4 * w;
+    if (lane == k0) mine = (int)(lo & 0xFFFFu);
+    if (lane == k0 + 1) mine = (int)(lo >> 16);
+    if (lane == k0 + 2) mine = (int)(hi & 0xFFFFu);
+    if (lane == k0 + 3) mine = (int)(hi >> 16);
+  }
+  return mine;
+}
+
+// COUNT of a two-level pass: tile t's 31 class counts go to its row of
+// tileCnt; the warp's running class totals of the segment (accSeg / accCnt,
+// lane k holds class k) go to the segment when the warp moves on.
+template <typename U, bool kIdx>
+__device__ __forceinline__ void count31_tile_warp(const SortArgs& a, int pass, int t,
+                                                  typename Persist<U, kIdx>::WarpArea& ws,
+                                                  unsigned& phases, int& accSeg, int& accCnt) {
+  using P = Persist<U, kIdx>;
+  using KT = typename P::KT;
+  constexpr int kItems = P::kItems, kWCH = P::kWCH, kShift = P::kTileShift;
+  static_assert(P::kTile / 32 < 256, "per-lane tile counts are 8-bit");
+  const int par = pass & 1;
+  const int lane = threadIdx.x & 31;
+  const U* src = (const U*)(par ? a.keysB : a.keysA);
+  const KT flip = (KT)a.flip;
+  const TileDesc td = load_tile(&a.tiles[par][t]);
+  const long long abs0 = (td.lo >> kShift) << kShift;
+  const int rlo = (int)(td.lo - abs0), rhi = (int)(td.hi - abs0);
+  const int chBeg = rlo / kWCH, chEnd = (rhi + kWCH - 1) / kWCH;
+  if (lane == 0 && chunk_bulk_ok<U, false>(src, nullptr, abs0 + (long long)chBeg * kWCH, a.n))
+    chunk_bulk_issue<U, kIdx, false>(ws, 0, src, nullptr, abs0 + (long long)chBeg * kWCH);
+  if (td.seg != ws.t.pivSeg) {  // pivots of the warp's last segment are kept
+    wide_pivots_warp<KT>(&a.segs[par][td.seg], &ws.t.wp);
+    ws.t.pivSeg = td.seg;
+  }
+  const PivotSet<KT> pp = ws.t.wp.par;
+  const PivotSet<KT>* child = ws.t.wp.child;
+  unsigned acc8[8];
+#pragma unroll
+  for (int w = 0; w < 8; ++w) acc8[w] = 0;
+  for (int ch = chBeg; ch < chEnd; ++ch) {
+    const int b = (ch - chBeg) & 1;
+    const long long c0 = abs0 + (long long)ch * kWCH;
+    if (ch + 1 < chEnd && lane == 0 && chunk_bulk_ok<U, false>(src, nullptr, c0 + kWCH, a.n))
+      chunk_bulk_issue<U, kIdx, false>(ws, b ^ 1, src, nullptr, c0 + kWCH);
+    const int e0 = ch * kWCH + lane * kItems;
+    KT key[kItems];
+    unsigned okm = 0;
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) okm |= (e0 + i >= rlo && e0 + i < rhi) ? (1u << i) : 0u;
+    if (chunk_bulk_ok<U, false>(src, nullptr, c0, a.n)) {
+      chunk_wait<U, kIdx>(ws, b, phases, a.ctrl);
+      chunk_keys<U, kIdx>(ws, b, lane, flip, key);
+    } else {
+      load_chunk<U, KT, kItems>(src + abs0, abs0, a.n, e0, rlo, rhi, flip, key);
+    }
+    unsigned acc4[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+    for (int i = 0; i < kItems; ++i)
+      if (okm >> i & 1u) wide_bump(acc4, wide_class_of<KT>(key[i], pp, child));
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+      acc8[2 * w] += widen_lo(acc4[w]);
+      acc8[2 * w + 1] += widen_hi(acc4[w]);
+    }
+    __syncwarp();
+  }
+  const int mine = wide_totals(acc8);
+  a.tileCnt[par][(long long)t * kRow + lane] = mine;
+  if (td.seg != accSeg) {
+    if (accSeg >= 0 && accCnt) atomicAdd(&a.segs[par][accSeg].tot[lane], accCnt);
+    accSeg = td.seg;
+    accCnt = 0;
+  }
+  accCnt += mine;
+}
+
+// PLAN of a two-level pass, one plan item (kThreads tiles of one segment):
+// the destination of every tile and class (class bases from the segment's
+// class totals, then the tiles in memory order: stable).  Item 0 also stores
+// the pivots for SCATTER and routes the 31 classes: the parent's pivot runs
+// and the children's pivot runs are parked for a fill when the keys go to the
+// scratch buffer; a child of at most kLeafMax keys becomes one leaf whatever
+// its second-level classes; every other grandchild becomes a leaf or a
+// next-pass segment.
+template <typename U, bool kIdx>
+__device__ __noinline__ void plan31_item(const SortArgs& a, int pass, int item,
+                                         typename Persist<U, kIdx>::Smem& sm) {
+  using P = Persist<U, kIdx>;
+  using KT = typename P::KT;
+  constexpr int kTile = P::kTile, kLeafMax = P::kLeafMax;
+  static_assert(kLeafMax >= kWideSamples, "segments hold at least kWideSamples keys");
+  const int par = pass & 1;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int seg = __ldcg(&a.planSeg[par][item]);
+  SegDesc* sdp = &a.segs[par][seg];
+  const int j = item - __ldcg(&sdp->planBase);
+  const long long sdStart = __ldcg(&sdp->start);
+  const int tileBase = __ldcg(&sdp->tileBase);
+  const int nt = __ldcg(&sdp->ntiles);
+  const int* cnt = a.tileCnt[par] + (long long)tileBase * kRow;
+  const int t0 = j * kThreads;
+  const int myTile = t0 + tid;
+  if (tid < 32) {
+    int x = tid < kWideClasses ? __ldcg(&sdp->tot[tid]) : 0;
+    const int tot = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(kFull, x, o);
+      if (lane >= o) x += y;
+    }
+    sm.wcb[tid] = x - tot;  // class start relative to the segment
+    if (tid == 31) sm.wcb[32] = x;
+  }
+  if (j == 0 && warp == 1) wide_pivots_warp<KT>(sdp, &sm.wpiv);
+  // offsets, eight classes per round
+  for (int g = 0; g < 4; ++g) {
+    int pre[8], v[8], inc[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) { pre[c] = 0; v[c] = 0; }
+#pragma unroll 4
+    for (int t = tid; t < t0; t += kThreads) {
+      const int4* row = reinterpret_cast<const int4*>(cnt + (long long)t * kRow + 8 * g);
+      const int4 x = __ldcg(row), y = __ldcg(row + 1);
+      pre[0] += x.x; pre[1] += x.y; pre[2] += x.z; pre[3] += x.w;
+      pre[4] += y.x; pre[5] += y.y; pre[6] += y.z; pre[7] += y.w;
+    }
+    if (myTile < nt) {
+      const int4* row = reinterpret_cast<const int4*>(cnt + (long long)myTile * kRow + 8 * g);
+      const int4 x = __ldcg(row), y = __ldcg(row + 1);
+      v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+      v[4] = y.x; v[5] = y.y; v[6] = y.z; v[7] = y.w;
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const int ps = (int)__reduce_add_sync(kFull, (unsigned)pre[c]);
+      int x = v[c];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(kFull, x, o);
+        if (lane >= o) x += y;
+      }
+      inc[c] = x;
+      if (lane == 31) { sm.red[warp][c] = x; sm.redPre[warp][c] = ps; }
+    }
+    __syncthreads();
+    if (tid < 8) {
+      int acc = 0, pacc = 0;
+      for (int w = 0; w < kWarps; ++w) {
+        const int x = sm.red[w][tid];
+        sm.red[w][tid] = acc;
+        acc += x;
+        pacc += sm.redPre[w][tid];
+      }
+      sm.pre[tid] = pacc;
+    }
+    __syncthreads();
+    if (myTile < nt) {
+      longlong2* dst = reinterpret_cast<longlong2*>(a.tileOff[par] +
+                                                    (long long)(tileBase + myTile) * kRow + 8 * g);
+#pragma unroll
+      for (int c = 0; c < 8; c += 2) {
+        const long long o0 =
+            sdStart + sm.wcb[8 * g + c] + sm.pre[c] + sm.red[warp][c] + (inc[c] - v[c]);
+        const long long o1 = sdStart + sm.wcb[8 * g + c + 1] + sm.pre[c + 1] +
+                             sm.red[warp][c + 1] + (inc[c + 1] - v[c + 1]);
+        dst[c / 2] = make_longlong2(o0, o1);
+      }
+    }
+    __syncthreads();
+  }
+  if (j != 0) return;
+
+  // item 0: routing (warp 0, lane k = class k)
+  const bool dstIsA = (par == 1);
+  const int nextPar = par ^ 1;
+  if (warp == 0) {
+    const int k = lane, ci = k >> 3, jj = k & 7;
+    unsigned park = 0u;
+    if (k < kWideClasses) {
+      const long long pos = sdStart + sm.wcb[k];
+      const long long m = sm.wcb[k + 1] - sm.wcb[k];
+      const long long cStart = sdStart + sm.wcb[8 * ci];
+      const long long cN = (long long)sm.wcb[8 * ci + 7] - sm.wcb[8 * ci];  // child ci
+      const bool leafChild = cN <= kLeafMax;
+      if (jj == 7) {  // the parent's pivot run ci
+        if (m > 0 && !dstIsA) {
+          push_fill(a, pos, m, (unsigned long long)sm.wpiv.par.p[ci]);
+          park = 1u;
+        }
+      } else if (leafChild) {
+        if (jj == 0) {
+          if (cN > 1 || (cN == 1 && !dstIsA)) push_leaf(a, cStart, cN, dstIsA ? 0 : 1);
+          for (int q = 0; q < 4; ++q) sm.gSeg[ci * 4 + q] = -1;
+        }
+      } else if (jj & 1) {  // child ci's pivot run jj/2
+        if (m > 0 && !dstIsA) {
+          push_fill(a, pos, m, (unsigned long long)sm.wpiv.child[ci].p[jj >> 1]);
+          park = 1u;
+        }
+      } else {  // grandchild g
+        const int g = ci * 4 + (jj >> 1);
+        int si = -1;
+        if (m > 1 || (m == 1 && !dstIsA)) {
+          if (m <= kLeafMax) {
+            push_leaf(a, pos, m, dstIsA ? 0 : 1);
+          } else {
+            int tb = 0, ntc = 0;
+            si = alloc_segment<kTile>(a, nextPar, pos, m, &tb, &ntc);
+            if (si >= 0) a.segs[nextPar][si].nsamp = kWideSamples;
+            sm.gTb[g] = tb;
+            sm.gNt[g] = si >= 0 ? ntc : 0;
+            sm.gStart[g] = pos;
+            sm.gN[g] = m;
+          }
+        }
+        sm.gSeg[g] = si;
+      }
+      sdp->cbase[k] = pos;
+    } else {
+      sdp->cbase[31] = sdStart + sm.wcb[32];
+    }
+    const unsigned pm = __ballot_sync(kFull, park != 0u);
+    if (lane == 0) {
+      sdp->parkMask = pm;
+      for (int q = 0; q < 3; ++q) sdp->pivS[q] = (unsigned long long)sm.wpiv.par.p[q];
+      sdp->lut = sm.wpiv.par.lut;
+      for (int c = 0; c < 4; ++c) {
+        for (int q = 0; q < 3; ++q) sdp->cpiv[c][q] = (unsigned long long)sm.wpiv.child[c].p[q];
+        sdp->clut[c] = sm.wpiv.child[c].lut;
+      }
+    }
+  }
+  __syncthreads();
+  if (tid < 16) sdp->childSeg[tid] = sm.gSeg[tid];
+  for (int g = 0; g < 16; ++g) {
+    if (sm.gSeg[g] >= 0)
+      write_tiles<kTile>(a, nextPar, sm.gSeg[g], sm.gTb[g], sm.gNt[g], sm.gStart[g], sm.gN[g],
+                         tid, kThreads);
+  }
+  __syncthreads();
+}
+
+// SCATTER of a two-level pass: scatter_tile_warp with 31 classes.  Lane
+// counts are 4-bit fields of four words (word = child), the warp scan runs on
+// eight words of 8-bit fields, the class starts come from a lane scan of the
+// class totals, and each lane's stage slots per class (8-bit fields of eight
+// words) sit in shared memory.  Lane k also watches the sample positions of
+// grandchild class k and copies the staged key written there into the new
+// segment's samples.
+template <typename U, bool kIdx>
+__device__ __forceinline__ void scatter31_tile_warp(const SortArgs& a, int pass, int t,
+                                                    typename Persist<U, kIdx>::WarpArea& ws,
+                                                    unsigned& phases) {
+  using P = Persist<U, kIdx>;
+  using KT = typename P::KT;
+  constexpr int kItems = P::kItems, kWCH = P::kWCH, kShift = P::kTileShift;
+  const int par = pass & 1;
+  const KT flip = (KT)a.flip;
+  const int lane = threadIdx.x & 31;
+  const TileDesc td = load_tile(&a.tiles[par][t]);
+  const long long abs0 = (td.lo >> kShift) << kShift;
+  const int rlo = (int)(td.lo - abs0), rhi = (int)(td.hi - abs0);
+  const U* srcK = (const U*)(par ? a.keysB : a.keysA);
+  const int* srcI = par ? a.idxB : a.idxA;
+  const int chBeg = rlo / kWCH, chEnd = (rhi + kWCH - 1) / kWCH;
+  if (lane == 0 && chunk_bulk_ok<U, kIdx>(srcK, srcI, abs0 + (long long)chBeg * kWCH, a.n))
+    chunk_bulk_issue<U, kIdx, true>(ws, 0, srcK, srcI, abs0 + (long long)chBeg * kWCH);
+  const SegDesc* sdp = &a.segs[par][td.seg];
+  if (td.seg != ws.t.pivSeg) {
+    if (lane == 0) {
+      WidePivots<KT> wp;
+      for (int q = 0; q < 3; ++q) wp.par.p[q] = (KT)__ldcg(&sdp->pivS[q]);
+      wp.par.lut = __ldcg(&sdp->lut);
+      for (int c = 0; c < 4; ++c) {
+        for (int q = 0; q < 3; ++q) wp.child[c].p[q] = (KT)__ldcg(&sdp->cpiv[c][q]);
+        wp.child[c].lut = __ldcg(&sdp->clut[c]);
+      }
+      ws.t.wp = wp;
+    }
+    ws.t.pivSeg = td.seg;
+  }
+  const unsigned parkMask = __ldcg(&sdp->parkMask);
+  {
+    // running destination of class `lane`, and its next sample position
+    const long long wb = __ldcg(&a.tileOff[par][(long long)t * kRow + lane]);
+    ws.t.wbase[lane] = wb;
+    long long nextP = LLONG_MAX;
+    int nextI = 0;
+    const int jj = lane & 7;
+    if (lane < kWideClasses && jj < 7 && !(jj & 1)) {
+      const int gs = __ldcg(&sdp->childSeg[(lane >> 3) * 4 + (jj >> 1)]);
+      if (gs >= 0) {
+        const long long gpos = __ldcg(&sdp->cbase[lane]);
+        const long long m = __ldcg(&sdp->cbase[lane + 1]) - gpos;
+        const long long r = wb - gpos;  // class rank of the tile's first key of the class
+        // first sample i with floor((2i+1) m / 2ns) >= r
+        const long long q = (2 * (long long)kWideSamples * r + m - 1) / m;
+        nextI = (int)(q / 2);
+        if (nextI < kWideSamples) nextP = wide_sample_pos(gpos, m, nextI, kWideSamples);
+      }
+    }
+    ws.t.capP[lane] = nextP;
+    ws.t.capI[lane] = nextI;
+  }
+  __syncwarp();
+  __syncwarp();
+  const PivotSet<KT> pp = ws.t.wp.par;
+  const PivotSet<KT>* child = ws.t.wp.child;
+  U* dstK = (U*)(par ? a.keysA : a.keysB);
+  int* dstI = par ? a.idxA : a.idxB;
+
+  for (int ch = chBeg; ch < chEnd; ++ch) {
+    const int b = (ch - chBeg) & 1;
+    const long long c0 = abs0 + (long long)ch * kWCH;
+    if (ch + 1 < chEnd && lane == 0 && chunk_bulk_ok<U, kIdx>(srcK, srcI, c0 + kWCH, a.n))
+      chunk_bulk_issue<U, kIdx, true>(ws, b ^ 1, srcK, srcI, c0 + kWCH);
+    const int e0 = ch * kWCH + lane * kItems;
+    KT key[kItems];
+    unsigned okm = 0;
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) okm |= (e0 + i >= rlo && e0 + i < rhi) ? (1u << i) : 0u;
+    if (chunk_bulk_ok<U, kIdx>(srcK, srcI, c0, a.n)) {
+      chunk_wait<U, kIdx>(ws, b, phases, a.ctrl);
+      chunk_keys<U, kIdx>(ws, b, lane, flip, key);
+    } else {
+      load_chunk<U, KT, kItems>(srcK + abs0, abs0, a.n, e0, rlo, rhi, flip, key);
+      if (kIdx) {
+        int id[kItems];
+        load_ids<kItems>(srcI + abs0, abs0, a.n, e0, okm, id);
+#pragma unroll
+        for (int i = 0; i < kItems; ++i) ws.pi[b][lane * kItems + i] = id[i];
+      }
+    }
+    // classes (5 bits each, 31 = no key) and in-lane ranks (4 bits each)
+    unsigned cwLo = 0, cwHi = 0, rw = 0;
+    unsigned acc4[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+      unsigned k = 31u;
+      if (okm >> i & 1u) {
+        k = wide_class_of<KT>(key[i], pp, child);
+        const unsigned w = k >> 3;
+        const unsigned x = w == 0u ? acc4[0] : w == 1u ? acc4[1] : w == 2u ? acc4[2] : acc4[3];
+        rw |= ((x >> (4u * (k & 7u))) & 15u) << (4 * i);
+        wide_bump(acc4, k);
+      }
+      if (i < 6) cwLo |= k << (5 * i);
+      else cwHi |= k << (5 * (i - 6));
+    }
+    // eight words of 8-bit fields (classes 4w..4w+3)
+    unsigned a8[8];
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+      a8[2 * w] = widen_lo(acc4[w]);
+      a8[2 * w + 1] = widen_hi(acc4[w]);
+    }
+    const int totk = wide_totals(a8);  // lane k: chunk total of class k
+    int csk = totk;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(kFull, csk, o);
+      if (lane >= o) csk += y;
+    }
+    const int nv = __shfl_sync(kFull, csk, 31);
+    csk -= totk;  // lane k: start of class k in the stage
+    // stage slot words: the class starts of classes 4w..4w+3 plus the lane's
+    // exclusive prefix within each class (warp scan of packed 8-bit fields;
+    // exclusive sums stay below 256, so the packed arithmetic is exact)
+    const unsigned mineCs = (unsigned)csk << (8 * (lane & 3));
+    unsigned grp = mineCs + __shfl_xor_sync(kFull, mineCs, 1);
+    grp += __shfl_xor_sync(kFull, grp, 2);
+#pragma unroll
+    for (int w = 0; w < 8; ++w) {
+      unsigned s = a8[w];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(kFull, s, o);
+        if (lane >= o) s += y;
+      }
+      ws.t.bword[w][lane] = __shfl_sync(kFull, grp, 4 * w) + (s - a8[w]);
+    }
+    // destination table of the chunk: delta[k] = running base - class start
+    const long long wbLo = ws.t.wbase[lane];
+    ws.t.delta[lane] = wbLo - (long long)csk;
+    ws.t.wbase[lane] = wbLo + totk;
+    __syncwarp();
+    // stage by class
+#pragma unroll
+    for (int h = 0; h < kItems; h += 4) {
+      int4 idv = make_int4(0, 0, 0, 0);
+      if (kIdx) idv = *reinterpret_cast<const int4*>(&ws.pi[b][lane * kItems + h]);
+      const int idq[4] = {idv.x, idv.y, idv.z, idv.w};
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int i = h + u;
+        const unsigned k = i < 6 ? (cwLo >> (5 * i)) & 31u : (cwHi >> (5 * (i - 6))) & 31u;
+        if (k != 31u) {
+          const unsigned pos =
+              ((ws.t.bword[k >> 2][lane] >> (8u * (k & 3u))) & 0xFFu) + ((rw >> (4 * i)) & 15u);
+          ws.sk[pos] = key[i];
+          if (kIdx) ws.si[pos] = idq[u];
+          ws.sc[pos] = (unsigned char)k;
+        }
+      }
+    }
+    __syncwarp();
+    // write-out: consecutive stage slots of one class go to consecutive addresses
+#pragma unroll
+    for (int jw = 0; jw < kItems; ++jw) {
+      const int sl = 32 * jw + lane;
+      if (sl < nv) {
+        const unsigned k = ws.sc[sl];
+        const long long d = ws.t.delta[k] + sl;
+        if (!((parkMask >> k) & 1u)) dstK[d] = U(ws.sk[sl] ^ flip);
+        if (kIdx) dstI[d] = ws.si[sl];
+      }
+    }
+    // samples of grandchild class `lane` written by this chunk
+    {
+      long long nextP = ws.t.capP[lane];
+      const long long hiP = wbLo + totk;
+      if (nextP < hiP) {
+        const int gs = __ldcg(&sdp->childSeg[(lane >> 3) * 4 + ((lane & 7) >> 1)]);
+        const long long gpos = __ldcg(&sdp->cbase[lane]);
+        const long long m = __ldcg(&sdp->cbase[lane + 1]) - gpos;
+        int nextI = ws.t.capI[lane];
+        SegDesc* gd = &a.segs[par ^ 1][gs];
+        while (nextP < hiP) {
+          gd->samp[nextI] = (unsigned long long)ws.sk[csk + (int)(nextP - wbLo)];
+          ++nextI;
+          nextP = nextI < kWideSamples ? wide_sample_pos(gpos, m, nextI, kWideSamples) : LLONG_MAX;
+        }
+        ws.t.capP[lane] = nextP;
+        ws.t.capI[lane] = nextI;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+}  // namespace turtle
