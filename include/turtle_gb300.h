@@ -75,7 +75,10 @@ int turtle_compression_ok(const turtle_sorter* s);
  * (turtle-sort.cuh:124-184): copies n keys (and n int32 ids when idx is not
  * NULL) from host memory and starts the sort asynchronously.  The host
  * buffers must stay valid until turtle_sync returns; results are written back
- * into them by turtle_sync. */
+ * into them by the time turtle_sync returns.  When both buffers are pinned
+ * (cudaHostAlloc / cudaHostRegister) and n >= 4M, the result is copied back
+ * slice by slice while the rest of the array is still being sorted; the
+ * buffers' contents are then unspecified if turtle_sync reports an error. */
 turtle_status turtle_start(turtle_sorter* s, void* host_keys, int32_t* host_idx, int64_t n);
 
 /* Replaces double Sync() (turtle-sort.cuh:188-258): waits for the sort,
@@ -262,6 +265,12 @@ int turtle_debug_kernel_times(turtle_sorter* s, int last, double* partition_ms, 
  * 4 = a work list was full; block = the CTA; info = site detail.  Returns
  * the device status word (0 = no error). */
 int turtle_debug_error_site(const turtle_sorter* s, int* site, int* block, int* info);
+
+/* For testing the yield path: later sorts on this sorter stop the partition
+ * and drain the leaf lists (leaf launches, then a resumed partition) whenever
+ * more than `leaves` leaves are pending at the start of a level.  0 restores
+ * the default (yield only when the lists could overflow). */
+turtle_status turtle_debug_yield_threshold(turtle_sorter* s, int32_t leaves);
 
 /* Library version string (static storage). */
 const char* turtle_version(void);

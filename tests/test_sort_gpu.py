@@ -250,3 +250,71 @@ def test_two_level_passes(dtype, dist):
         s.StartSorting(ko)
         s.Sync()
         assert np.array_equal(ko, np.sort(k, kind="stable"))
+
+
+def _pinned(dtype, n):
+    """A pinned host array of n elements (torch pinned bytes viewed as dtype)."""
+    import torch
+    t = torch.empty(n * np.dtype(dtype).itemsize, dtype=torch.uint8, pin_memory=True)
+    return t, t.numpy().view(dtype)
+
+
+@pytest.mark.parametrize("dtype,track", [(np.int32, True), (np.uint64, False), (np.int16, True),
+                                         (np.int64, True)])
+def test_overlapped_result_copies(dtype, track):
+    """Pinned buffers of at least 4M keys: the result comes back slice by slice
+    while later slices are still being sorted; it must equal the stable sort."""
+    n = (1 << 22) + 12345
+    s = TurtleSort(dtype, n, track_index=track)
+    for dist, seed in [("uniform", 11), ("dups", 12), ("sorted", 13)]:
+        keys = make_keys(dtype, n, dist, seed)
+        kt, kb = _pinned(dtype, n)
+        kb[:] = keys
+        it, ib = (None, None)
+        idx0 = None
+        if track:
+            idx0 = np.arange(n, dtype=np.int32)[::-1].copy()
+            it, ib = _pinned(np.int32, n)
+            ib[:] = idx0
+        launches = s.launches
+        s.StartSorting(kb, ib)
+        s.Sync()
+        assert s.launches - launches > 2  # partition + one leaf launch per slice
+        check_sorted_pair(keys, kb, ib, idx0)
+    s.close()
+
+
+@pytest.mark.parametrize("rule", ["sampled", "reference", "two_level"])
+@pytest.mark.parametrize("pinned", [False, True])
+def test_yield_and_resume(rule, pinned):
+    """The partition stops to drain the leaf lists and resumes where it left
+    off (forced by a low yield threshold); the result is unchanged, also when
+    the result copies were already queued slice by slice."""
+    n = (1 << 22) + 777
+    s = TurtleSort(np.int32, n, track_index=True)
+    s.set_pivot_rule(rule)
+    plain = s.launches
+    keys = make_keys(np.int32, n, "uniform", 21)
+    ko = keys.copy()
+    s.StartSorting(ko)
+    s.Sync()
+    plain = s.launches - plain
+    s.yield_threshold(64)
+    for dist, seed in [("uniform", 21), ("dups", 22), ("organ", 23)]:
+        keys = make_keys(np.int32, n, dist, seed)
+        idx0 = np.arange(n, dtype=np.int32)
+        if pinned:
+            kt, ko = _pinned(np.int32, n)
+            it, io = _pinned(np.int32, n)
+            ko[:] = keys
+            io[:] = idx0
+        else:
+            ko, io = keys.copy(), idx0.copy()
+        launches = s.launches
+        s.StartSorting(ko, io)
+        s.Sync()
+        if dist == "uniform":
+            assert s.launches - launches > plain  # it did yield
+        check_sorted_pair(keys, ko, io, idx0)
+    s.yield_threshold(0)
+    s.close()

@@ -231,6 +231,12 @@ class TurtleSort:
         later sort (see kernel_times)."""
         _check(self._lib.turtle_debug_time_kernels(self._h, int(enable)), "time_kernels", self._h)
 
+    def yield_threshold(self, leaves: int) -> None:
+        """Testing: yield to the leaf phase whenever more than ``leaves`` leaves
+        are pending (0 = only when the lists could overflow)."""
+        _check(self._lib.turtle_debug_yield_threshold(self._h, int(leaves)), "yield_threshold",
+               self._h)
+
     def kernel_times(self, last: int):
         """(sorts, partition_ms, leaf_ms) summed over the last `last` timed sorts."""
         pm, lm = C.c_double(), C.c_double()

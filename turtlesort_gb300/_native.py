@@ -58,6 +58,7 @@ SIGNATURES = [
     ("turtle_debug_time_kernels", _I, [_P, _I]),
     ("turtle_debug_kernel_times", _I, [_P, _I, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("turtle_debug_error_site", _I, [_P, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I)]),
+    ("turtle_debug_yield_threshold", _I, [_P, C.c_int32]),
     ("turtle_server_create", _I, [_I, _I64, _I, _I64, C.POINTER(_P)]),
     ("turtle_server_submit", _I, [_P, _I, _P, _P, _I64, C.POINTER(C.c_uint64)]),
     ("turtle_server_poll", _I, [_P, C.c_uint64, C.POINTER(_I)]),

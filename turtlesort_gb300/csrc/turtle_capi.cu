@@ -30,6 +30,10 @@ using turtle::dtype_flip;
 namespace {
 
 constexpr long long kMaxElements = (1LL << 31) - 1;  // int32 ids and in-segment offsets
+// StartSorting of at least this many keys into pinned host buffers sorts the
+// leaves in kMaxSlices position slices and copies each finished slice back
+// while the later slices are still being sorted.
+constexpr long long kOverlapMinKeys = 1LL << 22;
 
 }  // namespace
 
@@ -67,6 +71,12 @@ struct turtle_sorter {
   bool lastValid = false;
   cudaStream_t lastStream = nullptr;
   int pivotRule = turtle::kRuleSampled;
+  // overlapped device-to-host copies of StartSorting (pinned host buffers)
+  cudaStream_t copyStream = nullptr;
+  cudaEvent_t sliceEv[turtle::kMaxSlices] = {};
+  bool overlapped = false;  // this StartSorting's result copies are queued on copyStream
+  bool yielded = false;     // the partition yielded: those copies may be stale
+  int leafYield = 0;        // test threshold for yields (0: default)
   // optional kernel timing: events around the two launches of each sort
   static constexpr int kRing = 64;
   bool timeKernels = false;
@@ -105,9 +115,13 @@ turtle_status alloc_workspace(turtle_sorter* s, long long extraLeaves) {
 }
 
 turtle::SortArgs make_args(turtle_sorter* s, void* keys, int32_t* idx, const long long* offs,
-                           long long num, long long n) {
-  return turtle::bind_args(keys, idx, s->keysB.ptr, (int*)s->idxB.ptr, (char*)s->ws.ptr, s->lay,
-                           offs, num, n, s->flip, s->pivotRule);
+                           long long num, long long n, int slices = 1) {
+  turtle::SortArgs a = turtle::bind_args(keys, idx, s->keysB.ptr, (int*)s->idxB.ptr,
+                                         (char*)s->ws.ptr, s->lay, offs, num, n, s->flip,
+                                         s->pivotRule);
+  a.slices = slices;
+  a.leafYield = s->leafYield;
+  return a;
 }
 
 // Enqueue: reset the control block, run the persistent kernel, copy the
@@ -123,13 +137,14 @@ cudaError_t enqueue_persistent(turtle_sorter* s, const turtle::SortArgs& a, bool
   cudaError_t e = cudaSuccess;
   if (timing && (e = cudaEventRecord(ev[0], st)) != cudaSuccess) return e;
   e = turtle::kernels_launch_persistent(s->width, hasIdx, a, s->grid[hasIdx ? 1 : 0], st,
-                                        timing ? ev[1] : nullptr);
+                                        timing ? ev[1] : nullptr,
+                                        a.slices > 1 ? s->sliceEv : nullptr);
   if (e != cudaSuccess) return e;
   if (timing) {
     if ((e = cudaEventRecord(ev[2], st)) != cudaSuccess) return e;
     ++s->timed;
   }
-  s->launches.fetch_add(2);  // partition + leaf kernel
+  s->launches.fetch_add(1 + a.slices);  // partition + leaf launches
   s->lastArgs = a;
   s->lastArgs.resume = 1;
   s->lastHasIdx = hasIdx;
@@ -168,6 +183,7 @@ turtle_status finish_yields(turtle_sorter* s) {
   int rounds = 0;
   while (s->lastValid && s->hctrl->error == 0 && s->hctrl->yield != 0) {
     if (++rounds > 100000) return TURTLE_ERR_CAPACITY;
+    s->yielded = true;
     TRY_CUDA(s, enqueue_persistent(s, s->lastArgs, s->lastHasIdx, s->lastStream));
     TRY_CUDA(s, cudaStreamSynchronize(s->lastStream));
   }
@@ -175,11 +191,42 @@ turtle_status finish_yields(turtle_sorter* s) {
 }
 
 turtle_status sort_device_impl(turtle_sorter* s, void* keys, int32_t* idx, long long n,
-                               cudaStream_t st) {
+                               cudaStream_t st, int slices = 1) {
   if (n < 2) return TURTLE_OK;
   const bool hasIdx = idx != nullptr;
-  turtle::SortArgs a = make_args(s, keys, idx, nullptr, 0, n);
+  turtle::SortArgs a = make_args(s, keys, idx, nullptr, 0, n, slices);
   TRY_CUDA(s, enqueue_persistent(s, a, hasIdx, st));
+  return TURTLE_OK;
+}
+
+bool host_pinned(const void* p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeHost;
+}
+
+// Result copies of StartSorting: after leaf launch sl, keys [lo, hi) of slice
+// sl are final (the leaves of a slice start inside it), so copyStream brings
+// them back while the later slices are sorted.
+turtle_status queue_slice_copies(turtle_sorter* s, int slices) {
+  const long long n = s->n;
+  for (int sl = 0; sl < slices; ++sl) {
+    const long long lo = (sl * n + slices - 1) / slices;
+    const long long hi = ((sl + 1) * n + slices - 1) / slices;
+    TRY_CUDA(s, cudaStreamWaitEvent(s->copyStream, s->sliceEv[sl], 0));
+    if (hi <= lo) continue;
+    TRY_CUDA(s, cudaMemcpyAsync((char*)s->hostKeys + lo * s->width,
+                                (const char*)s->keysA.ptr + lo * s->width,
+                                (size_t)(hi - lo) * s->width, cudaMemcpyDeviceToHost,
+                                s->copyStream));
+    if (s->hostIdx)
+      TRY_CUDA(s, cudaMemcpyAsync(s->hostIdx + lo, (const int32_t*)s->idxA.ptr + lo,
+                                  (size_t)(hi - lo) * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                  s->copyStream));
+  }
   return TURTLE_OK;
 }
 
@@ -237,6 +284,11 @@ turtle_status turtle_create(turtle_dtype dtype, int64_t max_n, int track_index, 
   std::memset(s->hctrl, 0, sizeof(turtle::Control));
   if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess)
     return fail(from_cuda(s, e));
+  if ((e = cudaStreamCreateWithFlags(&s->copyStream, cudaStreamNonBlocking)) != cudaSuccess)
+    return fail(from_cuda(s, e));
+  for (auto& ev : s->sliceEv)
+    if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess)
+      return fail(from_cuda(s, e));
   if ((e = turtle::kernels_prepare(width, false, device, &s->grid[0])) != cudaSuccess)
     return fail(from_cuda(s, e));
   if ((e = turtle::kernels_prepare(width, true, device, &s->grid[1])) != cudaSuccess)
@@ -250,6 +302,9 @@ turtle_status turtle_destroy(turtle_sorter* s) {
   cudaSetDevice(s->device);
   if (s->stream) cudaStreamSynchronize(s->stream);
   if (s->lastStream) cudaStreamSynchronize(s->lastStream);
+  if (s->copyStream) cudaStreamSynchronize(s->copyStream);
+  for (auto& ev : s->sliceEv)
+    if (ev) { cudaEventDestroy(ev); ev = nullptr; }
   for (auto& r : s->ev)
     for (auto& e : r)
       if (e) { cudaEventDestroy(e); e = nullptr; }
@@ -262,6 +317,7 @@ turtle_status turtle_destroy(turtle_sorter* s) {
   turtle::vmm_free(&s->offsets);
   if (s->hctrl) cudaFreeHost(s->hctrl);
   if (s->stream) cudaStreamDestroy(s->stream);
+  if (s->copyStream) cudaStreamDestroy(s->copyStream);
   cudaGetLastError();
   delete s;
   return TURTLE_OK;
@@ -290,9 +346,18 @@ turtle_status turtle_start(turtle_sorter* s, void* host_keys, int32_t* host_idx,
       TRY_CUDA(s, cudaMemcpyAsync(s->idxA.ptr, host_idx, (size_t)n * sizeof(int32_t),
                                   cudaMemcpyHostToDevice, s->stream));
   }
+  const int slices = (n >= kOverlapMinKeys && host_pinned(host_keys) &&
+                      (!host_idx || host_pinned(host_idx)))
+                         ? turtle::kMaxSlices
+                         : 1;
+  s->yielded = false;
   st = sort_device_impl(s, s->keysA.ptr, host_idx ? (int32_t*)s->idxA.ptr : nullptr, n,
-                        s->stream);
+                        s->stream, slices);
   if (st != TURTLE_OK) return st;
+  if (slices > 1) {
+    if ((st = queue_slice_copies(s, slices)) != TURTLE_OK) return st;
+    s->overlapped = true;
+  }
   s->pending = true;
   return TURTLE_OK;
 }
@@ -304,8 +369,13 @@ turtle_status turtle_sync(turtle_sorter* s, double* seconds) {
   s->pending = false;
   TRY_CUDA(s, cudaStreamSynchronize(s->stream));
   turtle_status st = device_status(s);
+  const bool overlapped = s->overlapped;
+  s->overlapped = false;
+  // the slice copies finish before any copy below (they may be stale after
+  // a yield, and must not land on top of the final result)
+  if (overlapped) TRY_CUDA(s, cudaStreamSynchronize(s->copyStream));
   if (st != TURTLE_OK) return st;
-  if (s->n > 0) {
+  if (s->n > 0 && (!overlapped || s->yielded)) {
     TRY_CUDA(s, cudaMemcpyAsync(s->hostKeys, s->keysA.ptr, (size_t)s->n * s->width,
                                 cudaMemcpyDeviceToHost, s->stream));
     if (s->hostIdx)
@@ -556,6 +626,14 @@ int turtle_debug_error_site(const turtle_sorter* s, int* site, int* block, int* 
   if (block) *block = s->hctrl->errBlock;
   if (info) *info = s->hctrl->errInfo;
   return s->hctrl->error;
+}
+
+turtle_status turtle_debug_yield_threshold(turtle_sorter* s, int32_t leaves) {
+  if (!s || leaves < 0) return TURTLE_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->leafYield = leaves;
+  free_graphs(s);  // captured launches carry the old threshold
+  return TURTLE_OK;
 }
 
 const char* turtle_version(void) { return "turtle-gb300 0.1 (sm_103a)"; }

@@ -46,6 +46,7 @@ constexpr int kSamples = 15;             // evenly spaced pivot samples (one-lev
 constexpr int kWideSamples = 63;         // pivot samples of a segment in two-level passes
 constexpr int kRow = 32;                 // per-tile row: 32 class counts / offsets / sample keys
 constexpr int kLeafClasses = 10;         // group sizes 1, 2, 4, ..., 512 threads
+constexpr int kMaxSlices = 8;            // leaf phase split by position (one launch each)
 constexpr long long kSpinLimit = 40000000LL;  // bounded barrier spin iterations
 constexpr int kTimeline = 160;           // phase timestamps kept per launch
 
@@ -145,8 +146,8 @@ struct Control {
   int planCount[2];               // plan items per level parity
   int leafCount;
   int fillCount;
-  int classCount[16];
-  int classFill[16];
+  int classCount[kMaxSlices * 16];  // leaves per (slice, size class)
+  int classFill[kMaxSlices * 16];
   unsigned int work[4];           // ring of per-phase work counters
   unsigned int barCount;
   unsigned int barGen;
@@ -154,12 +155,12 @@ struct Control {
   int levels;
   int tlCount;                    // timeline entries written (block 0)
   int finished;                   // CTAs that reached the end of the kernel
-  int leafItems;                  // leaf work items left for the leaf kernel
-  int fillItems;                  // parked pivot-run fills left for the leaf kernel
-  int classItemsG[16];            // first leaf item of each size class
-  int classOffG[16];              // first sorted leaf of each size class
-  unsigned int leafWork;          // leaf-kernel work counter
-  int leafDone;                   // leaf-kernel CTAs finished
+  int leafItems[kMaxSlices];      // leaf work items of each slice
+  int fillItems;                  // parked pivot-run fills (done with slice 0)
+  int classItemsG[kMaxSlices * 16];  // first item of each (slice, size class) in its slice
+  int classOffG[kMaxSlices * 16];    // first sorted leaf of each (slice, size class)
+  unsigned int leafWork[kMaxSlices];  // leaf-kernel work counter of each slice
+  int leafDone;                   // leaf-kernel CTAs finished (all slices)
   int yield;                      // 1: partition stopped early to drain the leaf lists
   int resumeLevel;                // level to continue from after a yield
   int resumePhase;                // work-counter ring position at the yield
@@ -191,6 +192,8 @@ struct SortArgs {
   FillDesc* fills;
   int segCap, tileCap, leafCap, fillCap, planCap;
   int resume;                // 1: continue a partition that yielded
+  int slices;                // leaf launches, one per position slice (1..kMaxSlices)
+  int leafYield;             // > 0: yield when more leaves are pending (testing)
   int samples;               // pivot samples per segment: 3 (reference rule, one-level
                              // passes) or kWideSamples (sampled rule, two-level passes)
   Control* ctrl;

@@ -14,8 +14,11 @@ struct SortArgs;
 cudaError_t kernels_prepare(int width, bool hasIdx, int device, int* grid);
 // Launches the partition kernel and the leaf kernel on `stream`; when `mid`
 // is not null it is recorded between the two launches.
+// Partition kernel, then a.slices leaf launches; sliceDone[s] (optional) is
+// recorded after leaf launch s, when every key below slice s's end is final.
 cudaError_t kernels_launch_persistent(int width, bool hasIdx, const SortArgs& a, int grid,
-                                      cudaStream_t stream, cudaEvent_t mid = nullptr);
+                                      cudaStream_t stream, cudaEvent_t mid = nullptr,
+                                      const cudaEvent_t* sliceDone = nullptr);
 cudaError_t kernels_launch_multisort(int width, bool hasIdx, void* keys, int* idx,
                                      long long numArrays, int arrSize, unsigned long long flip,
                                      cudaStream_t stream);

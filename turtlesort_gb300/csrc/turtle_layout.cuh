@@ -114,6 +114,8 @@ inline SortArgs bind_args(void* keys, int* idx, void* keysB, int* idxB, char* ws
   a.planCap = L.planCap;
   a.ctrl = (Control*)(ws + L.offCtrl);
   a.samples = rule_samples(rule);
+  a.slices = 1;
+  a.leafYield = 0;
   return a;
 }
 

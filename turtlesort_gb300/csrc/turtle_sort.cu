@@ -112,8 +112,8 @@ struct Persist {
     long long childStart[4], childN[4];
     KT piv[3];
     unsigned lut;
-    int classOff[16];
-    int classItems[16];
+    int classOff[kMaxSlices * 16];  // leaf buckets: (slice, size class)
+    int classItems[kMaxSlices * 16];
     // two-level plan
     int wcb[33];                    // class starts relative to the segment
     int gSeg[16], gTb[16], gNt[16]; // the grandchild segments
@@ -844,52 +844,70 @@ namespace turtle {
 // leaf bucketing (end of the partition kernel)
 // ---------------------------------------------------------------------------
 
-// Bucket the leaves by size class (largest class first) and publish the leaf
-// work items in the control block.  Uses 2 grid barriers; returns false on
-// error.
+// Slice of a leaf or fill: the position slice holding its first key.  Leaf
+// launch s sorts the leaves of slice s (launch 0 also fills every parked
+// pivot run), so once launch s is done every key below the end of slice s is
+// final.
+__device__ __forceinline__ int leaf_slice(long long start, long long n, int slices) {
+  const long long s = (start * slices) / (n > 0 ? n : 1);
+  return (int)(s < slices - 1 ? s : slices - 1);
+}
+
+// Bucket the leaves by (slice, size class) -- slices in order, largest class
+// first within a slice -- and publish the leaf work items in the control
+// block.  Uses 2 grid barriers; returns false on error.
 template <typename U, bool kIdx>
 __device__ __noinline__ bool leaf_bucket(const SortArgs& a, typename Persist<U, kIdx>::Smem& sm) {
   constexpr int kItems = Geom<U>::kLItems;
+  constexpr int kB = kMaxSlices * 16;
   Control* c = a.ctrl;
   const int tid = threadIdx.x;
+  const int S = a.slices;
   const int nLeaves = ld_acquire_int(&c->leafCount);
   const int nFills = ld_acquire_int(&c->fillCount);
   const int nl = nLeaves < a.leafCap ? nLeaves : a.leafCap;
   const int nf = nFills < a.fillCap ? nFills : a.fillCap;
-  // bucket 1: class counts
-  if (tid < 16) sm.classItems[tid] = 0;
+  // bucket 1: counts
+  for (int b = tid; b < kB; b += kThreads) sm.classItems[b] = 0;
   __syncthreads();
-  for (int i = blockIdx.x * kThreads + tid; i < nl; i += gridDim.x * kThreads)
-    atomicAdd(&sm.classItems[leaf_class<kItems>(a.leaves[i].n)], 1);
+  for (int i = blockIdx.x * kThreads + tid; i < nl; i += gridDim.x * kThreads) {
+    const LeafDesc d = a.leaves[i];
+    atomicAdd(&sm.classItems[leaf_slice(d.start, a.n, S) * 16 + leaf_class<kItems>(d.n)], 1);
+  }
   __syncthreads();
-  if (tid < kLeafClasses && sm.classItems[tid]) atomicAdd(&c->classCount[tid], sm.classItems[tid]);
+  for (int b = tid; b < S * 16; b += kThreads)
+    if (sm.classItems[b]) atomicAdd(&c->classCount[b], sm.classItems[b]);
   if (!grid_barrier(c)) return false;
   timeline_mark(c, nl);
-  // bucket 2: scatter into per-class ranges (largest class first)
+  // bucket 2: scatter into per-bucket ranges
   if (tid == 0) {
     int acc = 0;
-    for (int k = kLeafClasses - 1; k >= 0; --k) {
-      sm.classOff[k] = acc;
-      acc += ld_acquire_int(&c->classCount[k]);
+    for (int s = 0; s < S; ++s) {
+      for (int k = kLeafClasses - 1; k >= 0; --k) {
+        sm.classOff[s * 16 + k] = acc;
+        acc += ld_acquire_int(&c->classCount[s * 16 + k]);
+      }
     }
   }
   __syncthreads();
   for (int i = blockIdx.x * kThreads + tid; i < nl; i += gridDim.x * kThreads) {
     const LeafDesc d = a.leaves[i];
-    const int k = leaf_class<kItems>(d.n);
-    const int pos = sm.classOff[k] + atomicAdd(&c->classFill[k], 1);
+    const int b = leaf_slice(d.start, a.n, S) * 16 + leaf_class<kItems>(d.n);
+    const int pos = sm.classOff[b] + atomicAdd(&c->classFill[b], 1);
     a.leavesSorted[pos] = d;
   }
   if (blockIdx.x == 0 && tid == 0) {
-    int acc = 0;
-    for (int k = kLeafClasses - 1; k >= 0; --k) {
-      const int groups = kLThreads >> k;
-      const int cnt = ld_acquire_int(&c->classCount[k]);
-      c->classItemsG[k] = acc;  // first item of class k
-      c->classOffG[k] = sm.classOff[k];
-      acc += (cnt + groups - 1) / groups;
+    for (int s = 0; s < S; ++s) {
+      int acc = 0;
+      for (int k = kLeafClasses - 1; k >= 0; --k) {
+        const int groups = kLThreads >> k;
+        const int cnt = ld_acquire_int(&c->classCount[s * 16 + k]);
+        c->classItemsG[s * 16 + k] = acc;  // first item of class k in slice s
+        c->classOffG[s * 16 + k] = sm.classOff[s * 16 + k];
+        acc += (cnt + groups - 1) / groups;
+      }
+      c->leafItems[s] = acc;
     }
-    c->leafItems = acc;
     c->fillItems = nf;
   }
   if (!grid_barrier(c)) return false;
@@ -960,10 +978,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
     if (blockIdx.x == 0 && tid == 0) {
       c->leafCount = 0;
       c->fillCount = 0;
-      c->leafWork = 0;
+      for (int k = 0; k < kMaxSlices; ++k) c->leafWork[k] = 0;
       c->leafDone = 0;
       c->yield = 0;
-      for (int k = 0; k < 16; ++k) { c->classCount[k] = 0; c->classFill[k] = 0; }
+      for (int k = 0; k < kMaxSlices * 16; ++k) { c->classCount[k] = 0; c->classFill[k] = 0; }
     }
   } else if (a.offsets == nullptr) {
     // init: route the input array (level-0 list is parity 0)
@@ -1006,7 +1024,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
     const int nplan = ld_acquire_int(&c->planCount[par]);
     if (nsegs == 0) break;
     if (level >= kMaxLevels) { if (tid == 0) set_error(c, kDevCapacity); return; }
-    if (ld_acquire_int(&c->leafCount) > a.leafCap - leafRoom ||
+    if (ld_acquire_int(&c->leafCount) > (a.leafYield > 0 ? a.leafYield : a.leafCap - leafRoom) ||
         ld_acquire_int(&c->fillCount) > a.fillCap - fillRoom) {
       if (blockIdx.x == 0 && tid == 0) {
         c->yield = 1;
@@ -1117,23 +1135,26 @@ __device__ void fill_run(const SortArgs& a, const FillDesc& f) {
 // The LEAF phase: sorts the leaves published by persistent_sort_kernel and
 // fills the parked pivot runs.  An ordinary launch (no grid barrier) with its
 // own register budget and the larger leaf CTA.
+// Launch `slice` handles the leaves of that position slice; launch 0 also
+// fills the parked pivot runs.
 template <typename U, bool kIdx>
-__global__ void __launch_bounds__(kLThreads, 2) leaf_kernel(SortArgs a) {
+__global__ void __launch_bounds__(kLThreads, 2) leaf_kernel(SortArgs a, int slice) {
   using P = Persist<U, kIdx>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   typename P::LeafSmem& sm = *reinterpret_cast<typename P::LeafSmem*>(smem_raw);
   Control* c = a.ctrl;
   const int tid = threadIdx.x;
   if (ld_acquire_int(&c->error) != 0) return;
-  unsigned* wc = &c->leafWork;
+  const int sb = slice * 16;
+  unsigned* wc = &c->leafWork[slice];
   if (tid < 16) {
-    sm.classItems[tid] = ld_acquire_int(&c->classItemsG[tid]);
-    sm.classOff[tid] = ld_acquire_int(&c->classOffG[tid]);
+    sm.classItems[tid] = ld_acquire_int(&c->classItemsG[sb + tid]);
+    sm.classOff[tid] = ld_acquire_int(&c->classOffG[sb + tid]);
   }
   if (tid == 0) sm.item = (int)atomicAdd(wc, 1u);
   __syncthreads();
-  const int leafItems = ld_acquire_int(&c->leafItems);
-  const int nf = ld_acquire_int(&c->fillItems);
+  const int leafItems = ld_acquire_int(&c->leafItems[slice]);
+  const int nf = slice == 0 ? ld_acquire_int(&c->fillItems) : 0;
   int it = sm.item;
   while (it < leafItems + nf) {
     unsigned nxt = 0;
@@ -1144,7 +1165,7 @@ __global__ void __launch_bounds__(kLThreads, 2) leaf_kernel(SortArgs a) {
       while (k > 0 && it >= sm.classItems[k - 1]) --k;
       const int groups = kLThreads >> k;
       const int first = sm.classOff[k] + (it - sm.classItems[k]) * groups;
-      const int last = sm.classOff[k] + ld_acquire_int(&c->classCount[k]);
+      const int last = sm.classOff[k] + ld_acquire_int(&c->classCount[sb + k]);
       const int end = first + groups < last ? first + groups : last;
       sort_leaf_group<U, kIdx>(a, k, first, end, sm);
     } else {
@@ -1156,7 +1177,8 @@ __global__ void __launch_bounds__(kLThreads, 2) leaf_kernel(SortArgs a) {
     it = sm.item;
   }
   __syncthreads();
-  if (tid == 0 && atomicAdd(&c->leafDone, 1) == (int)gridDim.x - 1) c->tEnd = global_ns();
+  if (tid == 0 && atomicAdd(&c->leafDone, 1) == (slice + 1) * (int)gridDim.x - 1)
+    c->tEnd = global_ns();
 }
 
 // ---------------------------------------------------------------------------
@@ -1250,7 +1272,7 @@ static cudaError_t prepare_persistent(int device, int* gridOut) {
 
 template <typename U, bool kIdx>
 static cudaError_t launch_persistent(const SortArgs& a, int grid, cudaStream_t stream,
-                                     cudaEvent_t mid) {
+                                     cudaEvent_t mid, const cudaEvent_t* sliceDone) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
   cfg.blockDim = dim3(kThreads);
@@ -1269,9 +1291,14 @@ static cudaError_t launch_persistent(const SortArgs& a, int grid, cudaStream_t s
   int sms = 0, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  leaf_kernel<U, kIdx><<<(unsigned)(sms > 0 ? 2 * sms : 2), kLThreads, leaf_smem_bytes<U, kIdx>(),
-                         stream>>>(a);
-  return cudaGetLastError();
+  for (int sl = 0; sl < a.slices; ++sl) {
+    leaf_kernel<U, kIdx><<<(unsigned)(sms > 0 ? 2 * sms : 2), kLThreads,
+                           leaf_smem_bytes<U, kIdx>(), stream>>>(a, sl);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (sliceDone != nullptr && (e = cudaEventRecord(sliceDone[sl], stream)) != cudaSuccess)
+      return e;
+  }
+  return cudaSuccess;
 }
 
 template <typename U, bool kIdx>
@@ -1307,8 +1334,10 @@ cudaError_t kernels_prepare(int width, bool hasIdx, int device, int* grid) {
 }
 
 cudaError_t kernels_launch_persistent(int width, bool hasIdx, const SortArgs& a, int grid,
-                                      cudaStream_t stream, cudaEvent_t mid) {
-  TURTLE_WIDTH_DISPATCH(width, hasIdx, (launch_persistent<U, I>(a, grid, stream, mid)));
+                                      cudaStream_t stream, cudaEvent_t mid,
+                                      const cudaEvent_t* sliceDone) {
+  TURTLE_WIDTH_DISPATCH(width, hasIdx,
+                        (launch_persistent<U, I>(a, grid, stream, mid, sliceDone)));
 }
 
 cudaError_t kernels_launch_multisort(int width, bool hasIdx, void* keys, int* idx,
