@@ -203,7 +203,7 @@ turtle_status turtle_server_destroy(turtle_server* srv);
  * the same whichever rule runs because every step is stable):
  *   TURTLE_PIVOTS_REFERENCE  sorted{a[start+n/2], a[start], a[stop]} per
  *                            segment, as the reference (turtle-sort.cu:641-655);
- *   TURTLE_PIVOTS_SAMPLED    the quartiles of 15 evenly spaced keys of the
+ *   TURTLE_PIVOTS_SAMPLED    the quartiles of 31 evenly spaced keys of the
  *                            segment (default): fewer partition levels;
  *   TURTLE_PIVOTS_TWO_LEVEL  passes that apply two levels at once (31 classes;
  *                            pivots from 63 evenly spaced keys): half the

@@ -203,7 +203,7 @@ def test_errors():
 @pytest.mark.parametrize("dtype", [np.int32, np.uint8, np.int64, np.uint16])
 def test_pivot_rules_give_the_same_result(dtype):
     """The reference pivot rule (median of start/middle/stop), the sampled rule
-    (quartiles of 15 evenly spaced keys) and the two-level passes (31 classes
+    (quartiles of 31 evenly spaced keys) and the two-level passes (31 classes
     per pass) must all produce the stable order: pivots and pass shape form
     the partition tree, never the output."""
     n = 700_001

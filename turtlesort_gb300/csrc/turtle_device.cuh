@@ -42,11 +42,12 @@ constexpr int kFillChunk = 1 << 16;      // pivot-run fill work unit (elements)
 constexpr int kDepthSwitch = TURTLE_DEPTH_SWITCH;  // levels of start/mid/stop pivots
                                          // before switching to sampled quartile pivots
 constexpr int kMaxLevels = 4096;         // hard cap on partition levels
-constexpr int kSamples = 15;             // evenly spaced pivot samples (one-level sampled rule)
+constexpr int kSamples = 31;             // evenly spaced pivot samples (one-level sampled rule)
 constexpr int kWideSamples = 63;         // pivot samples of a segment in two-level passes
 constexpr int kRow = 32;                 // per-tile row: 32 class counts / offsets / sample keys
 constexpr int kLeafClasses = 10;         // group sizes 1, 2, 4, ..., 512 threads
-constexpr int kMaxSlices = 8;            // leaf phase split by position (one launch each)
+constexpr int kMaxSlices = 8;
+constexpr int kSmallPlanTiles = 64;      // segments this small are planned by one warp            // leaf phase split by position (one launch each)
 constexpr long long kSpinLimit = 40000000LL;  // bounded barrier spin iterations
 constexpr int kTimeline = 160;           // phase timestamps kept per launch
 
@@ -106,7 +107,7 @@ struct SegDesc {        // a segment partitioned by the multi-CTA 3-pivot pass
   unsigned clut[4];     // two-level: their class tables
   long long cbase[32];  // class boundaries after planning (one-level: 8, two-level: 32)
   int childSeg[16];     // next-level segments (one-level: 4 children, two-level: 16 grandchildren)
-  int tot[32];          // class totals, summed by COUNT
+  alignas(16) int tot[32];  // class totals, summed by COUNT (zeroed with 16-byte stores)
   int planBase;         // first plan item of this segment
   unsigned parkMask;    // two-level: classes whose keys wait in B for a fill
 };
@@ -144,6 +145,8 @@ struct FillDesc {       // a pivot run parked in scratch: keys filled by value
 struct Control {
   unsigned long long segTile[2];  // packed (segments << 32 | tiles) per level parity
   int planCount[2];               // plan items per level parity
+  int planSmallCount[2];          // small segments (one warp plans each) per level parity
+  unsigned int smallWork;         // small-segment plan counter of the current level
   int leafCount;
   int fillCount;
   int classCount[kMaxSlices * 16];  // leaves per (slice, size class)
@@ -186,6 +189,8 @@ struct SortArgs {
   int* tileCnt[2];           // [tile][kRow]: one-level: #(k<p1), #(k<=p1), #(k<p2), #(k<=p2),
                              // #(k<p3), #(k<=p3), #keys; two-level: the 31 class counts
   long long* tileOff[2];     // [tile][kRow] global destination of each class
+  int* planSmall[2];         // one-level passes: segments of at most kSmallPlanTiles tiles,
+                             // each planned by one warp
   int* planSeg[2];           // segment of each plan item (kPartTile * kThreads keys)
   LeafDesc* leaves;
   LeafDesc* leavesSorted;

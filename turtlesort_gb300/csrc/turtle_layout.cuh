@@ -14,7 +14,7 @@ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 struct WsLayout {
   int segCap = 0, tileCap = 0, leafCap = 0, fillCap = 0, planCap = 0;
-  size_t offPlanSeg[2] = {0, 0};
+  size_t offPlanSeg[2] = {0, 0}, offPlanSmall[2] = {0, 0};
   size_t offCtrl = 0, offSegs[2] = {0, 0}, offTiles[2] = {0, 0}, offTileCnt[2] = {0, 0},
          offTileOff[2] = {0, 0};
   size_t offLeaves = 0, offLeavesSorted = 0, offFills = 0, bytes = 0;
@@ -44,6 +44,7 @@ inline WsLayout make_layout(long long maxN, int tile, int leafMax, long long ext
   for (int p = 0; p < 2; ++p) { L.offTileCnt[p] = o; o = align_up(o + tileCap * turtle::kRow * sizeof(int), 256); }
   for (int p = 0; p < 2; ++p) { L.offTileOff[p] = o; o = align_up(o + tileCap * turtle::kRow * sizeof(long long), 256); }
   for (int p = 0; p < 2; ++p) { L.offPlanSeg[p] = o; o = align_up(o + planCap * sizeof(int), 256); }
+  for (int p = 0; p < 2; ++p) { L.offPlanSmall[p] = o; o = align_up(o + segCap * sizeof(int), 256); }
   L.offLeaves = o; o = align_up(o + leafCap * sizeof(turtle::LeafDesc), 256);
   L.offLeavesSorted = o; o = align_up(o + leafCap * sizeof(turtle::LeafDesc), 256);
   L.offFills = o; o = align_up(o + fillCap * sizeof(turtle::FillDesc), 256);
@@ -103,6 +104,7 @@ inline SortArgs bind_args(void* keys, int* idx, void* keysB, int* idxB, char* ws
     a.tileCnt[p] = (int*)(ws + L.offTileCnt[p]);
     a.tileOff[p] = (long long*)(ws + L.offTileOff[p]);
     a.planSeg[p] = (int*)(ws + L.offPlanSeg[p]);
+    a.planSmall[p] = (int*)(ws + L.offPlanSmall[p]);
   }
   a.leaves = (LeafDesc*)(ws + L.offLeaves);
   a.leavesSorted = (LeafDesc*)(ws + L.offLeavesSorted);

@@ -38,6 +38,7 @@
 // the pivots (every step is stable, so the result equals a stable sort by
 // key).
 #include <cuda_runtime.h>
+#include <cstddef>
 #include <cstdint>
 #include <cstdio>
 
@@ -55,6 +56,11 @@ constexpr int kMergeClassMax = 4;
 constexpr bool kRadixLeaves = false;
 
 constexpr int ilog2(int x) { return x <= 1 ? 0 : 1 + ilog2(x >> 1); }
+#ifndef TURTLE_COUNT_RING
+#define TURTLE_COUNT_RING 2
+#endif
+constexpr int kMaxRing = 8;  // deepest COUNT chunk ring (bulk-copy barriers per warp)
+static_assert(TURTLE_COUNT_RING >= 2 && TURTLE_COUNT_RING <= kMaxRing, "COUNT ring depth");
 constexpr unsigned kFull = 0xffffffffu;
 
 template <typename U, bool kIdx>
@@ -81,7 +87,7 @@ struct Persist {
     struct OneLevel {               // tables of a one-level pass (7 classes)
       long long delta[8];           // destination minus stage slot, per class
       long long wbase[8];           // running destination per class
-      long long cpos[4][16];        // children's pivot sample positions
+      long long cpos[4][32];        // children's pivot sample positions
       int cseg[4];                  // the child segments (-1: none)
     };
     struct TwoLevel {               // tables of a two-level pass (31 classes)
@@ -97,8 +103,18 @@ struct Persist {
       OneLevel o;
       TwoLevel t;
     };
-    unsigned long long mbar[2];     // bulk-copy completion barriers
+    unsigned long long mbar[kMaxRing];  // bulk-copy completion barriers (one per slot)
   };
+  // COUNT reads keys only: its chunk ring spans pk, pi, sk and si (contiguous)
+  static constexpr int kChunkBytes = kWCH * (int)sizeof(U);
+  static constexpr int kRingBytes = 2 * kWCH * (int)sizeof(U) + 2 * (kIdx ? kWCH : 4) * 4 +
+                                    kWCH * (int)sizeof(KT) + (kIdx ? kWCH : 4) * 4;
+  // two slots measured fastest on GB300 (a 1 KB bulk copy per warp with one in
+  // flight streams at HBM speed; deeper rings streamed slower)
+  static constexpr int kCountRing = TURTLE_COUNT_RING < kRingBytes / kChunkBytes
+                                        ? TURTLE_COUNT_RING
+                                        : kRingBytes / kChunkBytes;
+  static_assert(kCountRing >= 2, "COUNT double-buffers at least");
 
   struct Smem {  // partition CTA
     WarpArea w[kWarps];
@@ -133,6 +149,23 @@ struct Persist {
     int classItems[16];
   };
 };
+
+template <typename U, bool kIdx>
+struct RingLayoutCheck {
+  using W = typename Persist<U, kIdx>::WarpArea;
+  static_assert(offsetof(W, sc) - offsetof(W, pk) == (size_t)Persist<U, kIdx>::kRingBytes,
+                "the COUNT ring spans pk, pi, sk and si without padding");
+  static_assert(offsetof(W, pk) % 16 == 0 && Persist<U, kIdx>::kChunkBytes % 16 == 0,
+                "bulk-copy destinations are 16-byte aligned");
+};
+template struct RingLayoutCheck<uint8_t, false>;
+template struct RingLayoutCheck<uint8_t, true>;
+template struct RingLayoutCheck<uint16_t, false>;
+template struct RingLayoutCheck<uint16_t, true>;
+template struct RingLayoutCheck<uint32_t, false>;
+template struct RingLayoutCheck<uint32_t, true>;
+template struct RingLayoutCheck<uint64_t, false>;
+template struct RingLayoutCheck<uint64_t, true>;
 
 template <typename U, bool kIdx>
 constexpr size_t persist_smem_bytes() {
@@ -192,18 +225,17 @@ __device__ __forceinline__ void segment_pivots(const SegDesc* sd, const U* src, 
   } else if (ns == 3) {
     sort3<KT>((KT)__ldcg(&sd->samp[0]), (KT)__ldcg(&sd->samp[1]), (KT)__ldcg(&sd->samp[2]), piv);
   } else {
-    KT v[kSamples];
-#pragma unroll
-    for (int i = 0; i < kSamples; ++i) v[i] = (KT)__ldcg(&sd->samp[i]);
-    // rank of each sample (ties by index): the ranks 3, 7, 11 are the quartiles
-#pragma unroll
+    // rank of each sample (ties by index): ranks ns/4, ns/2, 3ns/4 are the quartiles
     for (int i = 0; i < kSamples; ++i) {
+      const KT vi = (KT)__ldcg(&sd->samp[i]);
       int r = 0;
-#pragma unroll
-      for (int j = 0; j < kSamples; ++j) r += (v[j] < v[i]) || (v[j] == v[i] && j < i);
-      if (r == 3) piv[0] = v[i];
-      if (r == 7) piv[1] = v[i];
-      if (r == 11) piv[2] = v[i];
+      for (int j = 0; j < kSamples; ++j) {
+        const KT vj = (KT)__ldcg(&sd->samp[j]);
+        r += (vj < vi) || (vj == vi && j < i);
+      }
+      if (r == kSamples / 4) piv[0] = vi;
+      if (r == kSamples / 2) piv[1] = vi;
+      if (r == (3 * kSamples) / 4) piv[2] = vi;
     }
   }
 }
@@ -225,10 +257,11 @@ __device__ __forceinline__ void segment_pivots_warp(const SegDesc* sd, const U* 
     const KT w = __shfl_sync(kFull, v, j);
     r += (w < v) || (w == v && j < lane);
   }
+  static_assert(kSamples <= 32, "one sample per lane");
   const bool in = lane < kSamples;
-  const int l1 = __ffs(__ballot_sync(kFull, in && r == 3)) - 1;
-  const int l2 = __ffs(__ballot_sync(kFull, in && r == 7)) - 1;
-  const int l3 = __ffs(__ballot_sync(kFull, in && r == 11)) - 1;
+  const int l1 = __ffs(__ballot_sync(kFull, in && r == kSamples / 4)) - 1;
+  const int l2 = __ffs(__ballot_sync(kFull, in && r == kSamples / 2)) - 1;
+  const int l3 = __ffs(__ballot_sync(kFull, in && r == (3 * kSamples) / 4)) - 1;
   piv[0] = __shfl_sync(kFull, v, l1);
   piv[1] = __shfl_sync(kFull, v, l2);
   piv[2] = __shfl_sync(kFull, v, l3);
@@ -241,31 +274,38 @@ __device__ __forceinline__ long long tiles_of(long long start, long long n) {
 
 // Allocate a next-level segment (tile range allocated with the same 64-bit
 // atomic, so tileBase grows with the segment index).  Returns the segment
-// index or -1 on overflow.  The caller writes the tile descriptors.
+// index or -1 on overflow.  The caller writes the tile descriptors.  With
+// smallPlans, a segment of at most kSmallPlanTiles tiles goes to the list of
+// segments planned by one warp instead of getting CTA plan items.
 template <int kTile>
 __device__ int alloc_segment(const SortArgs& a, int par, long long start, long long n,
-                             int* tbOut, int* ntOut) {
+                             int* tbOut, int* ntOut, bool smallPlans) {
   const long long nt = tiles_of<kTile>(start, n);
   const unsigned long long old =
       atomicAdd(&a.ctrl->segTile[par], (1ull << 32) | (unsigned long long)nt);
   const int si = (int)(old >> 32);
   const long long tb = (long long)(old & 0xffffffffull);
-  const int np = (int)((nt + kThreads - 1) / kThreads);  // plan items
-  const int pb = atomicAdd(&a.ctrl->planCount[par], np);
-  if (si >= a.segCap || tb + nt > a.tileCap || pb + np > a.planCap) {
+  const bool small = smallPlans && nt <= kSmallPlanTiles;
+  const int np = small ? 0 : (int)((nt + kThreads - 1) / kThreads);  // plan items
+  const int pb = small ? atomicAdd(&a.ctrl->planSmallCount[par], 1)
+                       : atomicAdd(&a.ctrl->planCount[par], np);
+  if (si >= a.segCap || tb + nt > a.tileCap || (small ? pb >= a.segCap : pb + np > a.planCap)) {
     set_error(a.ctrl, kDevCapacity, kSiteCapacity, 1);
     return -1;
   }
-  SegDesc d;
-  d.start = start; d.n = n; d.tileBase = (int)tb; d.ntiles = (int)nt;
-  d.nsamp = 0;
-  d.pivS[0] = d.pivS[1] = d.pivS[2] = 0;
-  d.lut = 0;
-  for (int c = 0; c < 32; ++c) { d.cbase[c] = 0; d.tot[c] = 0; }
-  for (int c = 0; c < 16; ++c) d.childSeg[c] = -1;
-  d.planBase = pb;
-  d.parkMask = 0u;
-  a.segs[par][si] = d;
+  if (small) a.planSmall[par][pb] = si;
+  // only the fields read before the plan writes them: the samples come from
+  // the parent's scatter, pivots, class bases and children from the plan
+  SegDesc* d = &a.segs[par][si];
+  d->start = start;
+  d->n = n;
+  d->tileBase = (int)tb;
+  d->ntiles = (int)nt;
+  d->nsamp = 0;
+  d->planBase = small ? -1 : pb;
+  int4* tot = reinterpret_cast<int4*>(d->tot);  // COUNT adds into the class totals
+#pragma unroll
+  for (int c = 0; c < 8; ++c) tot[c] = make_int4(0, 0, 0, 0);
   for (int k = 0; k < np; ++k) a.planSeg[par][pb + k] = si;
   *tbOut = (int)tb;
   *ntOut = (int)nt;
@@ -331,7 +371,7 @@ __device__ void route_input(const SortArgs& a, long long start, long long n, boo
   if (n <= 1) return;
   if (n <= kLeafMax) { push_leaf(a, start, n, 0); return; }
   int tb = 0, nt = 0;
-  const int si = alloc_segment<kTile>(a, 0, start, n, &tb, &nt);
+  const int si = alloc_segment<kTile>(a, 0, start, n, &tb, &nt, a.samples != kWideSamples);
   if (si < 0) return;
   using KT = typename KeyCfg<U>::KT;
   const U* src = (const U*)a.keysA;
@@ -433,9 +473,20 @@ __device__ __forceinline__ void chunk_wait(typename Persist<U, kIdx>::WarpArea& 
 // COUNT phase: one tile per warp
 // ---------------------------------------------------------------------------
 
-// Tile t, counted by one warp against its segment's pivots, chunk by chunk
-// (the next chunk is bulk-copied into the other buffer while the current one
-// is counted); lanes 0..6 store the tile's predicate totals and key count.
+// Lane 0: bulk-copy the keys of the chunk at c0 into COUNT ring slot r.
+template <typename U, bool kIdx>
+__device__ __forceinline__ void ring_issue(typename Persist<U, kIdx>::WarpArea& ws, int r,
+                                           const U* src, long long c0) {
+  constexpr int kCB = Persist<U, kIdx>::kChunkBytes;
+  fence_proxy_async_smem();
+  mbar_arm(&ws.mbar[r], kCB);
+  bulk_g2s(reinterpret_cast<unsigned char*>(ws.pk) + r * kCB, src + c0, kCB, &ws.mbar[r]);
+}
+
+// Tile t, counted by one warp against its segment's pivots, chunk by chunk.
+// Up to kCountRing - 1 chunks are bulk-copied ahead into a ring of slots
+// (COUNT needs neither ids nor the stage, so the ring uses their shared
+// memory too); lanes 0..6 store the tile's predicate totals and key count.
 template <typename U, bool kIdx>
 __device__ __forceinline__ void count_tile_warp(const SortArgs& a, int level, int t,
                                                 typename Persist<U, kIdx>::WarpArea& ws,
@@ -443,6 +494,7 @@ __device__ __forceinline__ void count_tile_warp(const SortArgs& a, int level, in
   using P = Persist<U, kIdx>;
   using KT = typename P::KT;
   constexpr int kItems = P::kItems, kWCH = P::kWCH, kShift = P::kTileShift;
+  constexpr int kR = P::kCountRing, kCB = P::kChunkBytes;
   const int par = level & 1;
   const int lane = threadIdx.x & 31;
   const U* src = (const U*)(par ? a.keysB : a.keysA);
@@ -450,25 +502,50 @@ __device__ __forceinline__ void count_tile_warp(const SortArgs& a, int level, in
   const TileDesc td = load_tile(&a.tiles[par][t]);
   const long long abs0 = (td.lo >> kShift) << kShift;
   const int rlo = (int)(td.lo - abs0), rhi = (int)(td.hi - abs0);
+  const int chBeg = rlo / kWCH, chEnd = (rhi + kWCH - 1) / kWCH;
+  if (lane == 0) {
+    for (int q = 0; q < kR - 1 && chBeg + q < chEnd; ++q) {
+      const long long c0 = abs0 + (long long)(chBeg + q) * kWCH;
+      if (chunk_bulk_ok<U, false>(src, nullptr, c0, a.n)) ring_issue<U, kIdx>(ws, q, src, c0);
+    }
+  }
   KT piv[3];
   segment_pivots_warp<KT, U>(&a.segs[par][td.seg], src, level, flip, a.samples, piv);
-  const int chBeg = rlo / kWCH, chEnd = (rhi + kWCH - 1) / kWCH;
-  if (lane == 0 && chunk_bulk_ok<U, false>(src, nullptr, abs0 + (long long)chBeg * kWCH, a.n))
-    chunk_bulk_issue<U, kIdx, false>(ws, 0, src, nullptr, abs0 + (long long)chBeg * kWCH);
   unsigned w0 = 0, w1 = 0, w2 = 0;  // (k<p | k<=p << 16) for p1, p2, p3
+  int r = 0;                        // ring slot of chunk ch
   for (int ch = chBeg; ch < chEnd; ++ch) {
-    const int b = (ch - chBeg) & 1;
     const long long c0 = abs0 + (long long)ch * kWCH;
-    if (ch + 1 < chEnd && lane == 0 && chunk_bulk_ok<U, false>(src, nullptr, c0 + kWCH, a.n))
-      chunk_bulk_issue<U, kIdx, false>(ws, b ^ 1, src, nullptr, c0 + kWCH);
+    {
+      // refill the slot freed by the previous chunk
+      const int ahead = ch + kR - 1;
+      const int ra = r == 0 ? kR - 1 : r - 1;
+      const long long ca = abs0 + (long long)ahead * kWCH;
+      if (ahead < chEnd && lane == 0 && chunk_bulk_ok<U, false>(src, nullptr, ca, a.n))
+        ring_issue<U, kIdx>(ws, ra, src, ca);
+    }
     const int e0 = ch * kWCH + lane * kItems;
     KT key[kItems];
-    unsigned okm = 0;
+    // keys of the lane inside the tile (every key of an interior chunk)
+    unsigned okm = (1u << kItems) - 1u;
+    if (ch * kWCH < rlo || (ch + 1) * kWCH > rhi) {
+      okm = 0;
 #pragma unroll
-    for (int i = 0; i < kItems; ++i) okm |= (e0 + i >= rlo && e0 + i < rhi) ? (1u << i) : 0u;
+      for (int i = 0; i < kItems; ++i) okm |= (e0 + i >= rlo && e0 + i < rhi) ? (1u << i) : 0u;
+    }
     if (chunk_bulk_ok<U, false>(src, nullptr, c0, a.n)) {
-      chunk_wait<U, kIdx>(ws, b, phases, a.ctrl);
-      chunk_keys<U, kIdx>(ws, b, lane, flip, key);
+      if (!mbar_wait(&ws.mbar[r], (phases >> r) & 1u))
+        set_error(a.ctrl, kDevTimeout, kSiteBulk, (int)(threadIdx.x >> 5) * 16 + r * 2 + (int)((phases >> r) & 1u));
+      phases ^= 1u << r;
+      constexpr int kBytes = kItems * (int)sizeof(U);
+      using V = typename std::conditional<kBytes % 16 == 0, uint4, uint2>::type;
+      V v[kBytes / (int)sizeof(V)];
+      const V* pk = reinterpret_cast<const V*>(reinterpret_cast<const unsigned char*>(ws.pk) +
+                                               r * kCB + lane * kBytes);
+#pragma unroll
+      for (int j = 0; j < kBytes / (int)sizeof(V); ++j) v[j] = pk[j];
+      const U* u = reinterpret_cast<const U*>(v);
+#pragma unroll
+      for (int i = 0; i < kItems; ++i) key[i] = KT(u[i]) ^ flip;
     } else {
       load_chunk<U, KT, kItems>(src + abs0, abs0, a.n, e0, rlo, rhi, flip, key);
     }
@@ -482,6 +559,7 @@ __device__ __forceinline__ void count_tile_warp(const SortArgs& a, int level, in
       }
     }
     __syncwarp();
+    r = r + 1 == kR ? 0 : r + 1;
   }
   w0 = __reduce_add_sync(kFull, w0);
   w1 = __reduce_add_sync(kFull, w1);
@@ -541,21 +619,33 @@ __device__ __noinline__ void plan_item(const SortArgs& a, int level, int item,
   const int* cnt = a.tileCnt[par] + (long long)tileBase * kRow;
   const int t0 = j * kThreads;
   if (tid < 7) sm.tot[tid] = __ldcg(&sdp->tot[tid]);
-  if (j == 0 && tid == 0) {
-    segment_pivots<KT, U>(sdp, (const U*)(par ? a.keysB : a.keysA), level, (KT)a.flip, a.samples,
-                          sm.piv);
-    sm.lut = pivot_lut(sm.piv[0] == sm.piv[1], sm.piv[1] == sm.piv[2]);
+  if (j == 0 && warp == 0) {
+    KT piv[3];
+    segment_pivots_warp<KT, U>(sdp, (const U*)(par ? a.keysB : a.keysA), level, (KT)a.flip,
+                               a.samples, piv);
+    if (lane == 0) {
+      sm.piv[0] = piv[0]; sm.piv[1] = piv[1]; sm.piv[2] = piv[2];
+      sm.lut = pivot_lut(piv[0] == piv[1], piv[1] == piv[2]);
+    }
   }
   // counts of the segment's tiles before this item, and of this thread's tile
+  // (the class map is additive over tiles: sum the raw predicate rows, then
+  // convert once)
   int pre[7], v[7];
-#pragma unroll
-  for (int c = 0; c < 7; ++c) { pre[c] = 0; v[c] = 0; }
-  for (int t = tid; t < t0; t += kThreads) {
-    int w[7];
-    tile_classes(cnt + (long long)t * kRow, w);
-#pragma unroll
-    for (int c = 0; c < 7; ++c) pre[c] += w[c];
+  {
+    int4 r0 = make_int4(0, 0, 0, 0), r1 = make_int4(0, 0, 0, 0);
+#pragma unroll 8
+    for (int t = tid; t < t0; t += kThreads) {
+      const int4* row = reinterpret_cast<const int4*>(cnt + (long long)t * kRow);
+      const int4 x = __ldcg(row), y = __ldcg(row + 1);
+      r0.x += x.x; r0.y += x.y; r0.z += x.z; r0.w += x.w;
+      r1.x += y.x; r1.y += y.y; r1.z += y.z;
+    }
+    const int pc[6] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y};
+    classes_from_predicates(pc, r1.z, pre);
   }
+#pragma unroll
+  for (int c = 0; c < 7; ++c) v[c] = 0;
   const int myTile = t0 + tid;
   if (myTile < nt) tile_classes(cnt + (long long)myTile * kRow, v);
   int inc[7];
@@ -622,7 +712,7 @@ __device__ __noinline__ void plan_item(const SortArgs& a, int level, int item,
           push_leaf(a, pos, m, dstIsA ? 0 : 1);
         } else {
           int tb = 0, ntc = 0;
-          si = alloc_segment<kTile>(a, nextPar, pos, m, &tb, &ntc);
+          si = alloc_segment<kTile>(a, nextPar, pos, m, &tb, &ntc, true);
           sm.childTb[ci] = tb;
           sm.childNt[ci] = si >= 0 ? ntc : 0;
           sm.childStart[ci] = pos;
@@ -644,6 +734,89 @@ __device__ __noinline__ void plan_item(const SortArgs& a, int level, int item,
                          sm.childStart[ci], sm.childN[ci], tid, kThreads);
   }
   __syncthreads();
+}
+
+// plan_item for a segment of at most kSmallPlanTiles tiles, by one warp (lane
+// l owns tiles 2l and 2l+1, so a warp scan gives the offsets in memory
+// order).  The deep levels hold thousands of such segments; one warp each
+// keeps the CTA's other warps planning other segments meanwhile.
+template <typename U, bool kIdx>
+__device__ __noinline__ void plan_small_warp(const SortArgs& a, int level, int seg) {
+  using P = Persist<U, kIdx>;
+  using KT = typename P::KT;
+  constexpr int kTile = P::kTile, kLeafMax = P::kLeafMax;
+  static_assert(kSmallPlanTiles == 64, "two tiles per lane");
+  const int par = level & 1;
+  const int lane = threadIdx.x & 31;
+  SegDesc* sdp = &a.segs[par][seg];
+  const long long sdStart = __ldcg(&sdp->start);
+  const int tileBase = __ldcg(&sdp->tileBase);
+  const int nt = __ldcg(&sdp->ntiles);
+  const int* cnt = a.tileCnt[par] + (long long)tileBase * kRow;
+  KT piv[3];
+  segment_pivots_warp<KT, U>(sdp, (const U*)(par ? a.keysB : a.keysA), level, (KT)a.flip,
+                             a.samples, piv);
+  const int t0 = 2 * lane, t1 = 2 * lane + 1;
+  int v0[7], v1[7];
+#pragma unroll
+  for (int c = 0; c < 7; ++c) { v0[c] = 0; v1[c] = 0; }
+  if (t0 < nt) tile_classes(cnt + (long long)t0 * kRow, v0);
+  if (t1 < nt) tile_classes(cnt + (long long)t1 * kRow, v1);
+  long long* off0 = a.tileOff[par] + (long long)(tileBase + t0) * kRow;
+  long long* off1 = off0 + kRow;
+  int base = 0, myBase = 0, myTot = 0;
+#pragma unroll
+  for (int c = 0; c < 7; ++c) {
+    const int sum = v0[c] + v1[c];
+    int x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(kFull, x, o);
+      if (lane >= o) x += y;
+    }
+    const int tot = __shfl_sync(kFull, x, 31);
+    const long long o = sdStart + base + (x - sum);
+    if (t0 < nt) off0[c] = o;
+    if (t1 < nt) off1[c] = o + v0[c];
+    if (lane == c) { myBase = base; myTot = tot; }
+    base += tot;
+  }
+  // lane c routes class c (fill, leaf or next-level segment)
+  const bool dstIsA = (par == 1);
+  const int nextPar = par ^ 1;
+  int si = -1, tb = 0, ntc = 0;
+  long long pos = 0, m = 0;
+  if (lane < 7) {
+    const int c = lane;
+    pos = sdStart + myBase;
+    m = myTot;
+    if (c & 1) {
+      if (m > 0 && !dstIsA) push_fill(a, pos, m, (unsigned long long)piv[c >> 1]);
+    } else {
+      if (m > 1 || (m == 1 && !dstIsA)) {
+        if (m <= kLeafMax) push_leaf(a, pos, m, dstIsA ? 0 : 1);
+        else si = alloc_segment<kTile>(a, nextPar, pos, m, &tb, &ntc, true);
+      }
+      sdp->childSeg[c >> 1] = si;
+    }
+    sdp->cbase[c] = pos;
+    if (c == 6) sdp->cbase[7] = sdStart + base;
+    if (c < 3) sdp->pivS[c] = (unsigned long long)piv[c];
+    if (c == 3) sdp->lut = pivot_lut(piv[0] == piv[1], piv[1] == piv[2]);
+  }
+  // tiles of the new segments
+#pragma unroll
+  for (int ci = 0; ci < 4; ++ci) {
+    const int s = __shfl_sync(kFull, si, 2 * ci);
+    if (s >= 0) {
+      const int ctb = __shfl_sync(kFull, tb, 2 * ci);
+      const int cnt2 = __shfl_sync(kFull, ntc, 2 * ci);
+      const long long cs = __shfl_sync(kFull, pos, 2 * ci);
+      const long long cn = __shfl_sync(kFull, m, 2 * ci);
+      write_tiles<kTile>(a, nextPar, s, ctb, cnt2, cs, cn, lane, 32);
+    }
+  }
+  __syncwarp();
 }
 
 // ---------------------------------------------------------------------------
@@ -685,18 +858,24 @@ __device__ __forceinline__ void scatter_tile_warp(const SortArgs& a, int level, 
   // running destination of each class; pivot positions of the children
   if (lane < 7) ws.o.wbase[lane] = __ldcg(&a.tileOff[par][(long long)t * kRow + lane]);
   const int ns = a.samples;
+  // lane 8*ci + j watches samples j, j+8, ... of child ci; it keeps the next
+  // one at or after the tile's first destination of the child's class
   const int myci = lane >> 3, myj = lane & 7;
-  bool watch = false;
+  int nextQ = 0;
+  long long nextPos = LLONG_MAX;
   {
     const int child = __ldcg(&sdp->childSeg[myci]);
-    if (child >= 0) {
+    if (myj == 0) ws.o.cseg[myci] = child;
+    if (child >= 0 && myj < ns) {
       const long long cb = __ldcg(&sdp->cbase[2 * myci]);
       const long long cn = __ldcg(&sdp->cbase[2 * myci + 1]) - cb;
-      if (myj < ns) ws.o.cpos[myci][myj] = sample_pos(cb, cn, myj, ns);
-      if (myj + 8 < ns) ws.o.cpos[myci][myj + 8] = sample_pos(cb, cn, myj + 8, ns);
-      watch = myj < ns;
+      const long long tStart = __ldcg(&a.tileOff[par][(long long)t * kRow + 2 * myci]);
+      for (int q = myj; q < ns; q += 8) {
+        const long long p = sample_pos(cb, cn, q, ns);
+        ws.o.cpos[myci][q] = p;
+        if (nextPos == LLONG_MAX && p >= tStart) { nextQ = q; nextPos = p; }
+      }
     }
-    if (myj == 0) ws.o.cseg[myci] = child;
   }
   __syncwarp();
 
@@ -707,9 +886,13 @@ __device__ __forceinline__ void scatter_tile_warp(const SortArgs& a, int level, 
       chunk_bulk_issue<U, kIdx, true>(ws, b ^ 1, srcK, srcI, c0 + kWCH);
     const int e0 = ch * kWCH + lane * kItems;  // tile-relative index of the lane's first key
     KT key[kItems];
-    unsigned okm = 0;
+    // keys of the lane inside the tile (every key of an interior chunk)
+    unsigned okm = (1u << kItems) - 1u;
+    if (ch * kWCH < rlo || (ch + 1) * kWCH > rhi) {
+      okm = 0;
 #pragma unroll
-    for (int i = 0; i < kItems; ++i) okm |= (e0 + i >= rlo && e0 + i < rhi) ? (1u << i) : 0u;
+      for (int i = 0; i < kItems; ++i) okm |= (e0 + i >= rlo && e0 + i < rhi) ? (1u << i) : 0u;
+    }
     if (chunk_bulk_ok<U, kIdx>(srcK, srcI, c0, a.n)) {
       chunk_wait<U, kIdx>(ws, b, phases, a.ctrl);
       chunk_keys<U, kIdx>(ws, b, lane, flip, key);
@@ -813,22 +996,17 @@ __device__ __forceinline__ void scatter_tile_warp(const SortArgs& a, int level, 
         }
       }
     }
-    // a child's pivot sample written by this chunk: copy its key
-    if (watch) {
-      const unsigned csA = myci == 0 ? 0u : myci == 1 ? cs2 : myci == 2 ? cs4 : cs6;
-      const unsigned csB = myci == 0 ? cs1 : myci == 1 ? cs3 : myci == 2 ? cs5 : nv;
-      if (csB > csA) {
-        const int child = ws.o.cseg[myci];
-        const long long dl = ws.o.delta[2 * myci];
-        long long r = ws.o.cpos[myci][myj] - dl;
-        if (r >= (long long)csA && r < (long long)csB)
-          a.segs[par ^ 1][child].samp[myj] = (unsigned long long)ws.sk[r];
-        if (myj + 8 < ns) {
-          r = ws.o.cpos[myci][myj + 8] - dl;
-          if (r >= (long long)csA && r < (long long)csB)
-            a.segs[par ^ 1][child].samp[myj + 8] = (unsigned long long)ws.sk[r];
-        }
-      }
+    // a child's pivot sample written by this chunk (its class run ends at the
+    // advanced base): copy the staged key
+    if (nextPos < ws.o.wbase[2 * myci]) {
+      const int child = ws.o.cseg[myci];
+      const long long dl = ws.o.delta[2 * myci];
+      const long long end = ws.o.wbase[2 * myci];
+      do {
+        a.segs[par ^ 1][child].samp[nextQ] = (unsigned long long)ws.sk[nextPos - dl];
+        nextQ += 8;
+        nextPos = nextQ < ns ? ws.o.cpos[myci][nextQ] : LLONG_MAX;
+      } while (nextPos < end);
     }
     __syncwarp();
   }
@@ -965,7 +1143,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
   const int tid = threadIdx.x;
   typename P::WarpArea& ws = sm.w[tid >> 5];
   unsigned mphase = 0;  // parity bit of each chunk buffer's barrier
-  if ((tid & 31) == 0) { mbar_init(&ws.mbar[0], 1); mbar_init(&ws.mbar[1], 1); }
+  if ((tid & 31) == 0)
+    for (int r = 0; r < kMaxRing; ++r) mbar_init(&ws.mbar[r], 1);
   __syncwarp();
   int phase = 0;
   int level = 0;
@@ -1052,6 +1231,17 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
         if (kWide) plan31_item<U, kIdx>(a, level, it, sm);
         else plan_item<U, kIdx>(a, level, it, sm);
       }
+      if (!kWide) {
+        // small segments: one warp each
+        const int nsmall = ld_acquire_int(&c->planSmallCount[par]);
+        for (;;) {
+          unsigned it = 0;
+          if ((tid & 31) == 0) it = atomicAdd(&c->smallWork, 1u);
+          it = __shfl_sync(kFull, it, 0);
+          if ((int)it >= nsmall) break;
+          plan_small_warp<U, kIdx>(a, level, __ldcg(&a.planSmall[par][it]));
+        }
+      }
       ++phase;
     }
     __threadfence();
@@ -1064,6 +1254,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
       // level+2 appends to it during the next PLAN phase
       st.store(0ull, cuda::memory_order_relaxed);
       c->planCount[par] = 0;
+      c->planSmallCount[par] = 0;
+      c->smallWork = 0;
       c->work[(phase + 2) & 3] = 0;
     }
     stream_tiles<U, kIdx, 1, kWide>(a, level, ntiles, &c->work[phase & 3], ws, mphase);

@@ -180,9 +180,13 @@ __device__ __forceinline__ void count31_tile_warp(const SortArgs& a, int pass, i
       chunk_bulk_issue<U, kIdx, false>(ws, b ^ 1, src, nullptr, c0 + kWCH);
     const int e0 = ch * kWCH + lane * kItems;
     KT key[kItems];
-    unsigned okm = 0;
+    // keys of the lane inside the tile (every key of an interior chunk)
+    unsigned okm = (1u << kItems) - 1u;
+    if (ch * kWCH < rlo || (ch + 1) * kWCH > rhi) {
+      okm = 0;
 #pragma unroll
-    for (int i = 0; i < kItems; ++i) okm |= (e0 + i >= rlo && e0 + i < rhi) ? (1u << i) : 0u;
+      for (int i = 0; i < kItems; ++i) okm |= (e0 + i >= rlo && e0 + i < rhi) ? (1u << i) : 0u;
+    }
     if (chunk_bulk_ok<U, false>(src, nullptr, c0, a.n)) {
       chunk_wait<U, kIdx>(ws, b, phases, a.ctrl);
       chunk_keys<U, kIdx>(ws, b, lane, flip, key);
@@ -341,7 +345,7 @@ __device__ __noinline__ void plan31_item(const SortArgs& a, int pass, int item,
             push_leaf(a, pos, m, dstIsA ? 0 : 1);
           } else {
             int tb = 0, ntc = 0;
-            si = alloc_segment<kTile>(a, nextPar, pos, m, &tb, &ntc);
+            si = alloc_segment<kTile>(a, nextPar, pos, m, &tb, &ntc, false);
             if (si >= 0) a.segs[nextPar][si].nsamp = kWideSamples;
             sm.gTb[g] = tb;
             sm.gNt[g] = si >= 0 ? ntc : 0;
@@ -452,9 +456,13 @@ __device__ __forceinline__ void scatter31_tile_warp(const SortArgs& a, int pass,
       chunk_bulk_issue<U, kIdx, true>(ws, b ^ 1, srcK, srcI, c0 + kWCH);
     const int e0 = ch * kWCH + lane * kItems;
     KT key[kItems];
-    unsigned okm = 0;
+    // keys of the lane inside the tile (every key of an interior chunk)
+    unsigned okm = (1u << kItems) - 1u;
+    if (ch * kWCH < rlo || (ch + 1) * kWCH > rhi) {
+      okm = 0;
 #pragma unroll
-    for (int i = 0; i < kItems; ++i) okm |= (e0 + i >= rlo && e0 + i < rhi) ? (1u << i) : 0u;
+      for (int i = 0; i < kItems; ++i) okm |= (e0 + i >= rlo && e0 + i < rhi) ? (1u << i) : 0u;
+    }
     if (chunk_bulk_ok<U, kIdx>(srcK, srcI, c0, a.n)) {
       chunk_wait<U, kIdx>(ws, b, phases, a.ctrl);
       chunk_keys<U, kIdx>(ws, b, lane, flip, key);
