@@ -171,7 +171,8 @@ typedef struct turtle_server_stats {
 /* Starts a server on `device` (< 0: current) that holds at most
  * hbm_budget_bytes of device memory for batches in flight.  A batch fuses at
  * most max_batch_requests requests (<= 0: 4096) and max_batch_keys keys
- * (<= 0: 2^25; a single larger request forms a batch alone). */
+ * (<= 0: 2^25; at most 2^31 - 1; a single larger request forms a batch
+ * alone). */
 turtle_status turtle_server_create(int device, int64_t hbm_budget_bytes, int max_batch_requests,
                                    int64_t max_batch_keys, turtle_server** out);
 

@@ -347,7 +347,8 @@ turtle_status turtle_server_create(int device, int64_t hbm_budget_bytes, int max
   s->device = device;
   s->budget = hbm_budget_bytes;
   if (max_batch_requests > 0) s->maxBatchRequests = max_batch_requests;
-  if (max_batch_keys > 0) s->maxBatchKeys = max_batch_keys;
+  // one launch addresses its keys with 32-bit positions
+  if (max_batch_keys > 0) s->maxBatchKeys = std::min<long long>(max_batch_keys, (1LL << 31) - 1);
   cudaSetDevice(device);
   cudaError_t e = cudaSuccess;
   for (int w : {1, 2, 4, 8})
