@@ -89,12 +89,15 @@ inline void check(turtle_status st, const char* where, const turtle_sorter* s = 
 #endif
 }
 
-// Key type -> turtle_dtype.  char follows the platform's signedness.
+// Key type -> turtle_dtype.  char follows the platform's signedness; float
+// and double sort in IEEE-754 totalOrder.
 template <typename T, size_t S = sizeof(T), bool Signed = std::is_signed<T>::value>
 struct dtype_of {
   static_assert(std::is_integral<T>::value && !std::is_same<T, bool>::value,
-                "TurtleSort on GB300 sorts integer keys (int8 .. uint64)");
+                "TurtleSort on GB300 sorts integer (int8 .. uint64), float and double keys");
 };
+template <> struct dtype_of<float, 4, true> { static const turtle_dtype value = TURTLE_FLOAT32; };
+template <> struct dtype_of<double, 8, true> { static const turtle_dtype value = TURTLE_FLOAT64; };
 template <typename T> struct dtype_of<T, 1, true> { static const turtle_dtype value = TURTLE_INT8; };
 template <typename T> struct dtype_of<T, 1, false> { static const turtle_dtype value = TURTLE_UINT8; };
 template <typename T> struct dtype_of<T, 2, true> { static const turtle_dtype value = TURTLE_INT16; };

@@ -20,7 +20,11 @@ extern "C" {
 
 /* Key types.  The reference instantiates its kernels for char, unsigned
  * char, short, unsigned short, int, unsigned, long, unsigned long
- * (turtle-sort.cu:956-1134); these are the same eight integer types. */
+ * (turtle-sort.cu:956-1134); these are the same eight integer types.  It also
+ * instantiates float and double (turtle-sort.cu:1136-1174), compared with <
+ * so that NaN placement is undefined; here they sort in IEEE-754 totalOrder:
+ * -NaN < -inf < ... < -0.0 < +0.0 < ... < +inf < +NaN, ties (equal bit
+ * patterns) in input order. */
 typedef enum turtle_dtype {
   TURTLE_INT8 = 0,
   TURTLE_UINT8 = 1,
@@ -29,7 +33,9 @@ typedef enum turtle_dtype {
   TURTLE_INT32 = 4,
   TURTLE_UINT32 = 5,
   TURTLE_INT64 = 6,
-  TURTLE_UINT64 = 7
+  TURTLE_UINT64 = 7,
+  TURTLE_FLOAT32 = 8,
+  TURTLE_FLOAT64 = 9
 } turtle_dtype;
 
 /* Status codes.  The reference aborts the process on any CUDA error

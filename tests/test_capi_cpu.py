@@ -40,6 +40,10 @@ def test_host_side_answers(native_lib):
     assert native_lib.turtle_max_elements(99, 1) == 0
     assert native_lib.turtle_smem_capacity(4, 1) == 8192
     assert native_lib.turtle_smem_capacity(6, 1) == 4096
+    assert native_lib.turtle_max_elements(8, 1) == (1 << 31) - 1  # float32
+    assert native_lib.turtle_smem_capacity(8, 1) == 8192
+    assert native_lib.turtle_smem_capacity(9, 1) == 4096          # float64
+    assert native_lib.turtle_max_elements(10, 1) == 0
     assert native_lib.turtle_version().startswith(b"turtle-gb300")
     # NULL handles are rejected, never dereferenced
     assert native_lib.turtle_sync(None, None) == 1

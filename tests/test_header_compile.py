@@ -34,7 +34,20 @@ int main() {
   Turtle::TurtleSort<long> wide(16);
   Turtle::TurtleSort<char> c8(16);
   Turtle::TurtleSort<short> s16(16);
-  return (ok && t >= 0 && s >= 0) ? 0 : 1;
+  // float keys, as the reference's main.cpp (MultiSort<float, 2038, 32>)
+  Turtle::TurtleSort<float> f32(32 * 2038);
+  std::vector<float> fv = {2.5f, -1.0f, 0.0f, -0.0f, 7.0f, -3.25f};
+  f32.StartSorting(&fv);
+  f32.Sync();
+  bool fok = true;
+  for (size_t i = 1; i < fv.size(); ++i) fok = fok && !(fv[i] < fv[i - 1]);
+  std::vector<float> farrays(32 * 2038);
+  for (size_t i = 0; i < farrays.size(); ++i) farrays[i] = (float)((i * 7919u) % 1000u) - 500.0f;
+  f32.MultiSort<float, 2038, 32>(32, farrays.data());
+  for (size_t a = 0; a < 32; ++a)
+    for (size_t i = 1; i < 2038; ++i) fok = fok && !(farrays[a * 2038 + i] < farrays[a * 2038 + i - 1]);
+  Turtle::TurtleSort<double, false> f64(16);
+  return (ok && fok && t >= 0 && s >= 0) ? 0 : 1;
 }
 '''
 

@@ -34,6 +34,8 @@ _DTYPES = {
     np.dtype(np.uint32): _native.UINT32,
     np.dtype(np.int64): _native.INT64,
     np.dtype(np.uint64): _native.UINT64,
+    np.dtype(np.float32): _native.FLOAT32,  # IEEE-754 totalOrder (NaNs by sign at the ends)
+    np.dtype(np.float64): _native.FLOAT64,
 }
 
 
@@ -44,7 +46,7 @@ def load_library():
 def dtype_code(dtype) -> int:
     dt = np.dtype(dtype)
     if dt not in _DTYPES:
-        raise TypeError(f"unsupported key dtype {dt} (integer types int8..uint64 only)")
+        raise TypeError(f"unsupported key dtype {dt} (int8..uint64, float32, float64)")
     return _DTYPES[dt]
 
 

@@ -12,7 +12,7 @@ from pathlib import Path
 LIB_PATH = Path(__file__).resolve().parent / "libturtle_gb300.so"
 
 # turtle_dtype
-INT8, UINT8, INT16, UINT16, INT32, UINT32, INT64, UINT64 = range(8)
+INT8, UINT8, INT16, UINT16, INT32, UINT32, INT64, UINT64, FLOAT32, FLOAT64 = range(10)
 
 STATUS = {
     0: "TURTLE_OK",

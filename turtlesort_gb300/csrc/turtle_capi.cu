@@ -117,7 +117,7 @@ turtle_status alloc_workspace(turtle_sorter* s, long long extraLeaves) {
 turtle::SortArgs make_args(turtle_sorter* s, void* keys, int32_t* idx, const long long* offs,
                            long long num, long long n, int slices = 1) {
   turtle::SortArgs a = turtle::bind_args(keys, idx, s->keysB.ptr, (int*)s->idxB.ptr,
-                                         (char*)s->ws.ptr, s->lay, offs, num, n, s->flip,
+                                         (char*)s->ws.ptr, s->lay, offs, num, n, s->dtype,
                                          s->pivotRule);
   a.slices = slices;
   a.leafYield = s->leafYield;
@@ -403,7 +403,8 @@ turtle_status turtle_multisort_device(turtle_sorter* s, void* d_keys, int32_t* d
   const int leafMax = turtle::kernels_leaf_max(s->width);
   if (arr_size <= leafMax) {
     TRY_CUDA(s, turtle::kernels_launch_multisort(s->width, d_idx != nullptr, d_keys, d_idx,
-                                                 num_arrays, (int)arr_size, s->flip, cs));
+                                                 num_arrays, (int)arr_size, s->flip,
+                                                 turtle::dtype_fbits(s->dtype), cs));
     s->launches.fetch_add(1);
     std::memset(s->hctrl, 0, sizeof(turtle::Control));
     return TURTLE_OK;

@@ -198,6 +198,7 @@ struct SortArgs {
   int segCap, tileCap, leafCap, fillCap, planCap;
   int resume;                // 1: continue a partition that yielded
   int slices;                // leaf launches, one per position slice (1..kMaxSlices)
+  int fbits;                 // float keys (32 / 64): sorted as totalOrder images, else 0
   int leafYield;             // > 0: yield when more leaves are pending (testing)
   int samples;               // pivot samples per segment: 3 (reference rule, one-level
                              // passes) or kWideSamples (sampled rule, two-level passes)

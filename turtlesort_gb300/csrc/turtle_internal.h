@@ -21,7 +21,7 @@ cudaError_t kernels_launch_persistent(int width, bool hasIdx, const SortArgs& a,
                                       const cudaEvent_t* sliceDone = nullptr);
 cudaError_t kernels_launch_multisort(int width, bool hasIdx, void* keys, int* idx,
                                      long long numArrays, int arrSize, unsigned long long flip,
-                                     cudaStream_t stream);
+                                     int fbits, cudaStream_t stream);
 int kernels_tile_elems(int width);
 int kernels_leaf_max(int width);
 

@@ -56,8 +56,8 @@ inline int dtype_width(int dt) {
   switch (dt) {
     case TURTLE_INT8: case TURTLE_UINT8: return 1;
     case TURTLE_INT16: case TURTLE_UINT16: return 2;
-    case TURTLE_INT32: case TURTLE_UINT32: return 4;
-    case TURTLE_INT64: case TURTLE_UINT64: return 8;
+    case TURTLE_INT32: case TURTLE_UINT32: case TURTLE_FLOAT32: return 4;
+    case TURTLE_INT64: case TURTLE_UINT64: case TURTLE_FLOAT64: return 8;
     default: return 0;
   }
 }
@@ -68,8 +68,15 @@ inline unsigned long long dtype_flip(int dt) {
     case TURTLE_INT16: return 0x8000ull;
     case TURTLE_INT32: return 0x80000000ull;
     case TURTLE_INT64: return 0x8000000000000000ull;
-    default: return 0ull;
+    default: return 0ull;  // unsigned keys; float keys are mapped by dtype_fbits
   }
+}
+
+// Float keys: bits of the IEEE-754 format (32 or 64), else 0.  The sort
+// kernels see float keys as their totalOrder images (an elementwise map
+// before the sort and its inverse after it).
+inline int dtype_fbits(int dt) {
+  return dt == TURTLE_FLOAT32 ? 32 : dt == TURTLE_FLOAT64 ? 64 : 0;
 }
 
 // Kernel arguments for sorting `keys` (+ `idx`) with scratch buffers
@@ -86,8 +93,8 @@ inline int rule_samples(int rule) {
 }
 
 inline SortArgs bind_args(void* keys, int* idx, void* keysB, int* idxB, char* ws, const WsLayout& L,
-                          const long long* offs, long long num, long long n,
-                          unsigned long long flip, int rule = kRuleSampled) {
+                          const long long* offs, long long num, long long n, int dtype,
+                          int rule = kRuleSampled) {
   SortArgs a;
   std::memset(&a, 0, sizeof(a));
   a.keysA = keys;
@@ -97,7 +104,8 @@ inline SortArgs bind_args(void* keys, int* idx, void* keysB, int* idxB, char* ws
   a.offsets = offs;
   a.numArrays = num;
   a.n = n;
-  a.flip = flip;
+  a.flip = dtype_flip(dtype);
+  a.fbits = dtype_fbits(dtype);
   for (int p = 0; p < 2; ++p) {
     a.segs[p] = (SegDesc*)(ws + L.offSegs[p]);
     a.tiles[p] = (TileDesc*)(ws + L.offTiles[p]);

@@ -157,7 +157,7 @@ turtle_status launch_batch(turtle_server* s, Batch* b) {
   cudaEventRecord(sl.inDone, s->sIn);
   // sort
   b->args = turtle::bind_args(keys, idx, keysB, idxB, ws, b->lay, offs, num, b->total,
-                              turtle::dtype_flip(b->dtype));
+                              b->dtype);
   cudaStreamWaitEvent(s->sSort, sl.inDone, 0);
   cudaMemsetAsync(b->args.ctrl, 0, sizeof(turtle::Control), s->sSort);
   e = turtle::kernels_launch_persistent(b->width, b->hasIdx, b->args,

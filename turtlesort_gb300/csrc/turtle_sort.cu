@@ -52,7 +52,8 @@ namespace turtle {
 // larger ones the radix groups of P / 32 warps.
 constexpr int kMergeClassMax = 4;
 // The merge-path groups measured faster than the radix groups for every leaf
-// class on GB300, so the radix groups are compiled out of the leaf sort.
+// class on GB300 (with digit peers found by match.any or by one vote per digit
+// bit), so the radix groups are compiled out of the leaf sort.
 constexpr bool kRadixLeaves = false;
 
 constexpr int ilog2(int x) { return x <= 1 ? 0 : 1 + ilog2(x >> 1); }
@@ -1427,6 +1428,45 @@ __global__ void __launch_bounds__(kLThreads, 2)
 }
 
 // ---------------------------------------------------------------------------
+// float keys: IEEE-754 totalOrder images
+// ---------------------------------------------------------------------------
+
+// keys[lo, hi) to their totalOrder images (negative: all bits flipped,
+// positive: sign bit set), or back with `inverse`.  As unsigned integers the
+// images order -NaN < -inf < ... < -0 < +0 < ... < +inf < +NaN.  With a
+// control block, the map back is skipped when the partition yielded (the keys
+// are still mid-sort; the resumed launch maps them back).
+template <typename U>
+__global__ void __launch_bounds__(256) float_order_kernel(U* keys, long long lo, long long hi,
+                                                          int inverse, Control* ctrl) {
+  if (ctrl != nullptr && ld_acquire_int(&ctrl->yield) != 0) return;
+  constexpr U kSign = U(1) << (8 * sizeof(U) - 1);
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = lo + (long long)blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += stride) {
+    const U b = keys[i];
+    const bool top = (b & kSign) != 0;
+    // forward: negative (top set) -> ~b, else b | sign; inverse: an image with
+    // the top bit set was positive -> b ^ sign, else -> ~b
+    const U mask = (top != (inverse != 0)) ? U(~U(0)) : kSign;
+    keys[i] = b ^ mask;
+  }
+}
+
+template <typename U>
+static cudaError_t launch_float_order(void* keys, long long lo, long long hi, bool inverse,
+                                      Control* ctrl, cudaStream_t stream) {
+  if (hi <= lo) return cudaSuccess;
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long want = (hi - lo + 255) / 256;
+  const long long cap = (long long)(sms > 0 ? sms : 1) * 8;
+  float_order_kernel<U><<<(unsigned)(want < cap ? want : cap), 256, 0, stream>>>(
+      (U*)keys, lo, hi, inverse ? 1 : 0, ctrl);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // host-side launchers
 // ---------------------------------------------------------------------------
 template <typename U, bool kIdx>
@@ -1465,6 +1505,11 @@ static cudaError_t prepare_persistent(int device, int* gridOut) {
 template <typename U, bool kIdx>
 static cudaError_t launch_persistent(const SortArgs& a, int grid, cudaStream_t stream,
                                      cudaEvent_t mid, const cudaEvent_t* sliceDone) {
+  constexpr bool kFloatable = sizeof(U) >= 4;  // float32 / float64 storage
+  cudaError_t e = cudaSuccess;
+  if (kFloatable && a.fbits != 0 && !a.resume &&
+      (e = launch_float_order<U>(a.keysA, 0, a.n, false, nullptr, stream)) != cudaSuccess)
+    return e;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
   cfg.blockDim = dim3(kThreads);
@@ -1475,9 +1520,9 @@ static cudaError_t launch_persistent(const SortArgs& a, int grid, cudaStream_t s
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  cudaError_t e = a.samples == kWideSamples
-                      ? cudaLaunchKernelEx(&cfg, persistent_sort_kernel<U, kIdx, true>, a)
-                      : cudaLaunchKernelEx(&cfg, persistent_sort_kernel<U, kIdx, false>, a);
+  e = a.samples == kWideSamples
+          ? cudaLaunchKernelEx(&cfg, persistent_sort_kernel<U, kIdx, true>, a)
+          : cudaLaunchKernelEx(&cfg, persistent_sort_kernel<U, kIdx, false>, a);
   if (e != cudaSuccess) return e;
   if (mid != nullptr && (e = cudaEventRecord(mid, stream)) != cudaSuccess) return e;
   int sms = 0, dev = 0;
@@ -1487,6 +1532,13 @@ static cudaError_t launch_persistent(const SortArgs& a, int grid, cudaStream_t s
     leaf_kernel<U, kIdx><<<(unsigned)(sms > 0 ? 2 * sms : 2), kLThreads,
                            leaf_smem_bytes<U, kIdx>(), stream>>>(a, sl);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (kFloatable && a.fbits != 0) {
+      // keys of this slice are final: back from totalOrder images
+      const long long lo = (sl * a.n + a.slices - 1) / a.slices;
+      const long long hi = ((sl + 1) * a.n + a.slices - 1) / a.slices;
+      if ((e = launch_float_order<U>(a.keysA, lo, hi, true, a.ctrl, stream)) != cudaSuccess)
+        return e;
+    }
     if (sliceDone != nullptr && (e = cudaEventRecord(sliceDone[sl], stream)) != cudaSuccess)
       return e;
   }
@@ -1495,16 +1547,24 @@ static cudaError_t launch_persistent(const SortArgs& a, int grid, cudaStream_t s
 
 template <typename U, bool kIdx>
 static cudaError_t launch_multisort(void* keys, int* idx, long long numArrays, int arrSize,
-                                    unsigned long long flip, cudaStream_t stream) {
+                                    unsigned long long flip, int fbits, cudaStream_t stream) {
   constexpr int kItems = Geom<U>::kLItems;
   int cls = 0;
   while ((1 << cls) * kItems < arrSize) ++cls;
   const int groups = kLThreads >> cls;
   const long long blocks = (numArrays + groups - 1) / groups;
   if (blocks <= 0) return cudaSuccess;
+  constexpr bool kFloatable = sizeof(U) >= 4;
+  const long long total = numArrays * (long long)arrSize;
+  cudaError_t e;
+  if (kFloatable && fbits != 0 &&
+      (e = launch_float_order<U>(keys, 0, total, false, nullptr, stream)) != cudaSuccess)
+    return e;
   multisort_kernel<U, kIdx><<<(unsigned)blocks, kLThreads, leaf_smem_bytes<U, kIdx>(), stream>>>(
       (U*)keys, idx, numArrays, arrSize, cls, flip);
-  return cudaGetLastError();
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (kFloatable && fbits != 0) return launch_float_order<U>(keys, 0, total, true, nullptr, stream);
+  return cudaSuccess;
 }
 
 // dispatch on key width / index
@@ -1534,9 +1594,9 @@ cudaError_t kernels_launch_persistent(int width, bool hasIdx, const SortArgs& a,
 
 cudaError_t kernels_launch_multisort(int width, bool hasIdx, void* keys, int* idx,
                                      long long numArrays, int arrSize, unsigned long long flip,
-                                     cudaStream_t stream) {
-  TURTLE_WIDTH_DISPATCH(width, hasIdx,
-                        (launch_multisort<U, I>(keys, idx, numArrays, arrSize, flip, stream)));
+                                     int fbits, cudaStream_t stream) {
+  TURTLE_WIDTH_DISPATCH(width, hasIdx, (launch_multisort<U, I>(keys, idx, numArrays, arrSize, flip,
+                                                               fbits, stream)));
 }
 
 int kernels_tile_elems(int width) {

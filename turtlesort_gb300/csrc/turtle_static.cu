@@ -113,8 +113,7 @@ extern "C" turtle_status turtle_sort_device_noalloc(turtle_dtype dtype, void* d_
   const bool hasIdx = d_idx != nullptr;
   cudaStream_t cs = (cudaStream_t)stream;
   turtle::SortArgs a = turtle::bind_args(d_keys, d_idx, st->base, (int*)(st->base + p.offIdx),
-                                         st->base + p.offWs, p.lay, nullptr, 0, n,
-                                         turtle::dtype_flip(dtype));
+                                         st->base + p.offWs, p.lay, nullptr, 0, n, dtype);
   // the previous call's work-list header must not leak into this one
   if ((e = cudaMemsetAsync(a.ctrl, 0, sizeof(turtle::Control), cs)) != cudaSuccess)
     return cuda_status(e);
