@@ -345,7 +345,7 @@ def main() -> None:
     ap.add_argument("--clocks-csv", default=None)
     ap.add_argument("--workload", default="sort64m",
                     choices=["sort64m", "plain12m", "sweep", "multisort", "batched", "wide",
-                             "serving"],
+                             "floats", "serving"],
                     help="sort64m (default) is the headline line; the others print their own")
     ap.add_argument("--requests", type=int, default=1000, help="serving: requests in the sample")
     ap.add_argument("--rate", type=float, default=0.0,

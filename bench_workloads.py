@@ -5,6 +5,7 @@
     python bench.py --workload multisort  # 262,144 arrays x 1024 int32
     python bench.py --workload batched    # 100,000 uneven arrays, int32 and int16
     python bench.py --workload wide       # int64 2^28 + idx, uint8 2^30, uint16 2^29 Zipf
+    python bench.py --workload floats     # 2^26 float32 + idx, 2^26 float64 + idx
     python bench.py --workload serving    # Poisson request stream through the server
 
 Every device-resident time is taken with CUDA events on the sorter's launch
@@ -156,6 +157,16 @@ def wide(args):
     del keys
     keys = dg.zipf_u16(1 << 29, dg.seed_for(3) + 2)
     _sort_line(args, "2^29 uint16 Zipf(1.1) over 65536 ranks, keys only", keys, None, "u16")
+
+
+def floats(args):
+    for dt, name in [(np.float32, "float32"), (np.float64, "float64")]:
+        rng = np.random.default_rng(dg.seed_for(4) + (4 if dt == np.float32 else 8))
+        keys = rng.standard_normal(1 << 26).astype(dt)
+        idx = np.arange(keys.size, dtype=np.int32)
+        _sort_line(args, f"2^26 {name} + int32 index, standard normal", keys, idx, name,
+                   "IEEE-754 totalOrder; numpy default_rng seeded normal values")
+        del keys, idx
 
 
 def multisort(args):
@@ -396,5 +407,6 @@ def serving(args):
                    "note": "pinned host buffers; host<->device copies inside every request"}})
 
 
-WORKLOADS = {"plain12m": plain12m, "sweep": sweep, "wide": wide, "multisort": multisort,
+WORKLOADS = {"plain12m": plain12m, "sweep": sweep, "wide": wide, "floats": floats,
+             "multisort": multisort,
              "batched": batched, "serving": serving}
