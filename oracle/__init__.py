@@ -50,9 +50,28 @@ def _p(a):
     return a.ctypes.data_as(C.c_void_p) if a is not None else None
 
 
+def total_order_image(x: np.ndarray) -> np.ndarray:
+    """Float keys -> unsigned images whose integer order is IEEE-754 totalOrder
+    (-NaN < -inf < ... < -0 < +0 < ... < +inf < +NaN): negative values have
+    every bit flipped, the others get the sign bit set."""
+    u = x.view(np.uint32 if x.dtype == np.float32 else np.uint64)
+    sign = u.dtype.type(1) << u.dtype.type(8 * u.itemsize - 1)
+    return np.where((u & sign) != 0, ~u, u | sign).astype(u.dtype)
+
+
+def from_total_order_image(u: np.ndarray, dtype) -> np.ndarray:
+    sign = u.dtype.type(1) << u.dtype.type(8 * u.itemsize - 1)
+    return np.where((u & sign) != 0, u ^ sign, ~u).astype(u.dtype).view(dtype)
+
+
 def turtle_sort(keys: np.ndarray, idx: np.ndarray | None = None, leaf_max: int = 8192,
                 threads: int = 1):
-    """Restated reference 3-pivot quicksort (stable tie order); returns copies."""
+    """Restated reference 3-pivot quicksort (stable tie order); returns copies.
+    Float keys (the reference's float/double instantiations,
+    turtle-sort.cu:1136-1174) are sorted as their totalOrder images."""
+    if keys.dtype in (np.float32, np.float64):
+        k, i = turtle_sort(total_order_image(np.ascontiguousarray(keys)), idx, leaf_max, threads)
+        return from_total_order_image(k, keys.dtype), i
     k = np.ascontiguousarray(keys).copy()
     i = None if idx is None else np.ascontiguousarray(idx, dtype=np.int32).copy()
     rc = lib().oracle_turtle_sort(_DT[k.dtype], _p(k), _p(i), k.size, leaf_max, threads)

@@ -17,6 +17,16 @@ from conftest import ROOT
 GOLDEN = ROOT / "tests" / "golden"
 
 
+def bits(a: np.ndarray) -> np.ndarray:
+    """Bit patterns of float keys (NaN payloads and signed zeros compared
+    exactly); integer keys unchanged."""
+    if a.dtype == np.float32:
+        return a.view(np.uint32)
+    if a.dtype == np.float64:
+        return a.view(np.uint64)
+    return a
+
+
 def load_cases():
     z = np.load(GOLDEN / "sort_cases.npz")
     for line in z["index"]:
@@ -26,7 +36,7 @@ def load_cases():
 
 def test_fixture_set_is_complete():
     seen = {(dt, dist) for _, dt, _, dist, _, _ in load_cases()}
-    assert len({dt for dt, _ in seen}) == 8
+    assert len({dt for dt, _ in seen}) == 10  # 8 integer types, float32, float64
     assert {"uniform", "dups", "extremes", "reverse"} <= {d for _, d in seen}
 
 
@@ -34,7 +44,7 @@ def test_oracle_reproduces_fixtures(oracle_mod):
     for tag, dt, n, dist, keys, perm in load_cases():
         idx = np.arange(n, dtype=np.int32)
         k, i = oracle_mod.turtle_sort(keys, idx, leaf_max=128)
-        assert np.array_equal(k, keys[perm]), tag
+        assert np.array_equal(bits(k), bits(keys[perm])), tag
         assert np.array_equal(i, perm), tag
 
 
@@ -51,10 +61,10 @@ def test_cuda_path_reproduces_fixtures(gpu):
             i = np.arange(n, dtype=np.int32)
             sorters[key].StartSorting(k, i)
             sorters[key].Sync()
-            assert np.array_equal(k, keys[perm]), f"{tag} {dt} {n} {dist}"
+            assert np.array_equal(bits(k), bits(keys[perm])), f"{tag} {dt} {n} {dist}"
             assert np.array_equal(i, perm), f"{tag} {dt} {n} {dist}"
             # ids initialised to the values (the reference README benchmark)
-            if np.dtype(dt).itemsize <= 4 and np.dtype(dt) != np.uint32:
+            if np.dtype(dt).kind in "iu" and np.dtype(dt).itemsize <= 4 and np.dtype(dt) != np.uint32:
                 k2 = keys.copy()
                 i2 = keys.astype(np.int32)
                 sorters[key].StartSorting(k2, i2)
