@@ -318,6 +318,8 @@ def run_gpu(args) -> None:
                 "d2h_bytes_per_step": n * 8,
                 "path": "turtle_start/turtle_sync (StartSorting/Sync) with pinned host buffers",
                 "ms_per_step": 1e3 * sum(e2e_t) / len(e2e_t),
+                "ms_min_median_max": [1e3 * min(e2e_t), 1e3 * sorted(e2e_t)[len(e2e_t) // 2],
+                                      1e3 * max(e2e_t)],
                 "gpu_launches_per_step": e2e_launches / len(e2e_t),
                 "overlap": "leaf phase in position slices; each finished slice is copied to the "
                            "host while later slices sort"},

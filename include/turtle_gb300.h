@@ -211,13 +211,16 @@ turtle_status turtle_server_destroy(turtle_server* srv);
  *   TURTLE_PIVOTS_REFERENCE  sorted{a[start+n/2], a[start], a[stop]} per
  *                            segment, as the reference (turtle-sort.cu:641-655);
  *   TURTLE_PIVOTS_SAMPLED    the quartiles of 31 evenly spaced keys of the
- *                            segment (default): fewer partition levels;
+ *                            segment: fewer partition levels;
  *   TURTLE_PIVOTS_TWO_LEVEL  passes that apply two levels at once (31 classes;
  *                            pivots from 63 evenly spaced keys): half the
- *                            passes over the data, more work per key. */
+ *                            passes over the data, more work per key;
+ *   TURTLE_PIVOTS_AUTO       (default) two-level passes for sorts of at least
+ *                            2^23 keys, the sampled rule for smaller ones. */
 #define TURTLE_PIVOTS_REFERENCE 0
 #define TURTLE_PIVOTS_SAMPLED 1
 #define TURTLE_PIVOTS_TWO_LEVEL 2
+#define TURTLE_PIVOTS_AUTO 3
 turtle_status turtle_set_pivot_rule(turtle_sorter* s, int rule);
 
 /* ---- introspection ---- */

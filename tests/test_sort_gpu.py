@@ -211,7 +211,7 @@ def test_pivot_rules_give_the_same_result(dtype):
         k = make_keys(dtype, n, dist, seed)
         idx = np.arange(n, dtype=np.int32)
         outs = []
-        for rule in ("reference", "sampled", "two_level"):
+        for rule in ("reference", "sampled", "two_level", "auto"):
             s = TurtleSort(dtype, n, track_index=True)
             s.set_pivot_rule(rule)
             ko, io = k.copy(), idx.copy()
@@ -317,4 +317,51 @@ def test_yield_and_resume(rule, pinned):
             assert s.launches - launches > plain  # it did yield
         check_sorted_pair(keys, ko, io, idx0)
     s.yield_threshold(0)
+    s.close()
+
+
+@pytest.mark.parametrize("dtype", [np.int32, np.uint8, np.int64, np.float32])
+@pytest.mark.parametrize("arr", [7, 100, 2038, 9000])
+def test_multisort_device_with_ids(dtype, arr):
+    """MultiSort with an id payload (not available in the reference,
+    README.md:46): every row sorted stably, its ids reordered with it.  Rows
+    up to the shared-memory capacity use the MultiSort kernel, longer rows
+    the batched partition path."""
+    import torch
+    num = 64 * 3
+    n = arr * num
+    if dtype == np.float32:
+        keys = np.random.default_rng(arr).standard_normal(n).astype(np.float32)
+    else:
+        keys = make_keys(dtype, n, "dups" if arr % 2 else "uniform", arr)
+    ids = np.arange(n, dtype=np.int32)
+    s = TurtleSort(dtype, n, track_index=True)
+    dk = torch.from_numpy(keys.copy()).cuda()
+    di = torch.from_numpy(ids.copy()).cuda()
+    st = torch.cuda.current_stream().cuda_stream
+    s.multisort_device(dk.data_ptr(), di.data_ptr(), arr, num, st)
+    s.status(st)
+    ko = dk.cpu().numpy().reshape(num, arr)
+    io = di.cpu().numpy().reshape(num, arr)
+    rows = keys.reshape(num, arr)
+    for r in range(num):
+        order = np.argsort(rows[r], kind="stable")
+        assert np.array_equal(ko[r], rows[r][order]), r  # no NaN in these rows
+        assert np.array_equal(io[r], (order + r * arr).astype(np.int32)), r
+    s.close()
+
+
+@pytest.mark.parametrize("dtype", [np.int32, np.uint64, np.int16])
+def test_default_rule_above_two_level_threshold(dtype):
+    """The default pivot rule switches to two-level passes from 2^23 keys up;
+    those sorts must be exact too (with and without ids)."""
+    n = (1 << 23) + 5
+    s = TurtleSort(dtype, n, track_index=True)
+    for dist, seed in [("uniform", 31), ("dups", 32), ("organ", 33)]:
+        k = make_keys(dtype, n, dist, seed)
+        idx = np.arange(n, dtype=np.int32)
+        ko, io = k.copy(), idx.copy()
+        s.StartSorting(ko, io)
+        s.Sync()
+        check_sorted_pair(k, ko, io, idx)
     s.close()

@@ -215,10 +215,11 @@ class TurtleSort:
         return int(self._lib.turtle_last_levels(self._h))
 
     def set_pivot_rule(self, rule: str) -> None:
-        """'sampled' (default: quartiles of 31 evenly spaced keys), 'reference'
-        (the reference's median of start/middle/stop keys) or 'two_level'
-        (passes of two levels, 31 classes); same output."""
-        code = {"reference": 0, "sampled": 1, "two_level": 2}[rule]
+        """'auto' (default: two-level passes from 2^23 keys up, else 'sampled'),
+        'sampled' (quartiles of 31 evenly spaced keys), 'reference' (the
+        reference's median of start/middle/stop keys) or 'two_level' (passes
+        of two levels, 31 classes); same output."""
+        code = {"reference": 0, "sampled": 1, "two_level": 2, "auto": 3}[rule]
         _check(self._lib.turtle_set_pivot_rule(self._h, code), "set_pivot_rule", self._h)
 
     def error_site(self):

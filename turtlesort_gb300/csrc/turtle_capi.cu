@@ -70,7 +70,7 @@ struct turtle_sorter {
   bool lastHasIdx = false;
   bool lastValid = false;
   cudaStream_t lastStream = nullptr;
-  int pivotRule = turtle::kRuleSampled;
+  int pivotRule = turtle::kRuleAuto;
   // overlapped device-to-host copies of StartSorting (pinned host buffers)
   cudaStream_t copyStream = nullptr;
   cudaEvent_t sliceEv[turtle::kMaxSlices] = {};
@@ -581,7 +581,7 @@ int turtle_debug_timeline(const turtle_sorter* s, uint64_t* ns, int32_t* info, i
 }
 
 turtle_status turtle_set_pivot_rule(turtle_sorter* s, int rule) {
-  if (!s || rule < turtle::kRuleReference || rule > turtle::kRuleTwoLevel)
+  if (!s || rule < turtle::kRuleReference || rule > turtle::kRuleAuto)
     return TURTLE_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lk(s->mu);
   free_graphs(s);  // captured launches hold the old rule

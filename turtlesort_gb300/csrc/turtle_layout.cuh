@@ -88,13 +88,15 @@ inline int dtype_fbits(int dt) {
 constexpr int kRuleReference = 0;
 constexpr int kRuleSampled = 1;
 constexpr int kRuleTwoLevel = 2;
+constexpr int kRuleAuto = 3;                      // two-level from kAutoTwoLevelKeys keys up
+constexpr long long kAutoTwoLevelKeys = 1LL << 23;  // measured crossover on GB300
 inline int rule_samples(int rule) {
   return rule == kRuleReference ? 3 : rule == kRuleTwoLevel ? kWideSamples : kSamples;
 }
 
 inline SortArgs bind_args(void* keys, int* idx, void* keysB, int* idxB, char* ws, const WsLayout& L,
                           const long long* offs, long long num, long long n, int dtype,
-                          int rule = kRuleSampled) {
+                          int rule = kRuleAuto) {
   SortArgs a;
   std::memset(&a, 0, sizeof(a));
   a.keysA = keys;
@@ -123,6 +125,7 @@ inline SortArgs bind_args(void* keys, int* idx, void* keysB, int* idxB, char* ws
   a.fillCap = L.fillCap;
   a.planCap = L.planCap;
   a.ctrl = (Control*)(ws + L.offCtrl);
+  if (rule == kRuleAuto) rule = n >= kAutoTwoLevelKeys ? kRuleTwoLevel : kRuleSampled;
   a.samples = rule_samples(rule);
   a.slices = 1;
   a.leafYield = 0;

@@ -95,7 +95,8 @@ struct Persist {
       long long delta[32];          // destination minus stage slot, per class
       long long wbase[32];          // running destination per class
       long long capP[32];           // next sample position of each grandchild class
-      unsigned bword[8][32];        // per lane: stage slot of its first key of each class
+      int cnt[32];                  // running count of each class in the chunk (ranking)
+      int cs[32];                   // start of each class in the stage
       int capI[32];                 // index of that sample
       WidePivots<KT> wp;            // pivots of segment pivSeg
       int pivSeg;
@@ -362,24 +363,25 @@ __device__ void push_fill(const SortArgs& a, long long start, long long n, unsig
 }
 
 // Route one input array at init: nothing, leaf, or level-0 segment (with its
-// pivot candidates; its tiles are written when writeTiles).
+// pivot candidates, unless the caller reads them; its tiles are written when
+// writeTiles).
 template <typename U, int kTile, int kLeafMax>
 __device__ void route_input(const SortArgs& a, long long start, long long n, bool writeTiles,
-                            int* siOut, int* tbOut, int* ntOut) {
+                            int* siOut, int* tbOut, int* ntOut, bool samples = true) {
   *siOut = -1;
   *tbOut = 0;
   *ntOut = 0;
   if (n <= 1) return;
   if (n <= kLeafMax) { push_leaf(a, start, n, 0); return; }
   int tb = 0, nt = 0;
-  const int si = alloc_segment<kTile>(a, 0, start, n, &tb, &nt, a.samples != kWideSamples);
+  const int si = alloc_segment<kTile>(a, 0, start, n, &tb, &nt, true);
   if (si < 0) return;
   using KT = typename KeyCfg<U>::KT;
   const U* src = (const U*)a.keysA;
   const KT flip = (KT)a.flip;
   SegDesc* sd = &a.segs[0][si];
   sd->nsamp = a.samples;
-  for (int i = 0; i < a.samples; ++i)
+  for (int i = 0; samples && i < a.samples; ++i)
     sd->samp[i] = (unsigned long long)kload<U, KT>(src, sample_pos(start, n, i, a.samples), flip);
   if (writeTiles) write_tiles<kTile>(a, 0, si, tb, nt, start, n, 0, 1);
   *siOut = si; *tbOut = tb; *ntOut = nt;
@@ -1168,12 +1170,15 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
     if (blockIdx.x == 0) {
       if (tid == 0) {
         int si, tb, nt;
-        route_input<U, kTile, kLeafMax>(a, 0, a.n, false, &si, &tb, &nt);
+        route_input<U, kTile, kLeafMax>(a, 0, a.n, false, &si, &tb, &nt, false);
         sm.childSeg[0] = si;
         sm.childTb[0] = tb;
         sm.childNt[0] = nt;
       }
       __syncthreads();
+      if (sm.childSeg[0] >= 0 && tid < a.samples)  // pivot candidates, one per thread
+        a.segs[0][sm.childSeg[0]].samp[tid] = (unsigned long long)kload<U, typename P::KT>(
+            (const U*)a.keysA, sample_pos(0, a.n, tid, a.samples), (typename P::KT)a.flip);
       if (sm.childSeg[0] >= 0)
         write_tiles<kTile>(a, 0, sm.childSeg[0], sm.childTb[0], sm.childNt[0], 0, a.n, tid,
                            kThreads);
@@ -1232,7 +1237,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
         if (kWide) plan31_item<U, kIdx>(a, level, it, sm);
         else plan_item<U, kIdx>(a, level, it, sm);
       }
-      if (!kWide) {
+      {
         // small segments: one warp each
         const int nsmall = ld_acquire_int(&c->planSmallCount[par]);
         for (;;) {
@@ -1240,7 +1245,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
           if ((tid & 31) == 0) it = atomicAdd(&c->smallWork, 1u);
           it = __shfl_sync(kFull, it, 0);
           if ((int)it >= nsmall) break;
-          plan_small_warp<U, kIdx>(a, level, __ldcg(&a.planSmall[par][it]));
+          if (kWide) plan31_small_warp<U, kIdx>(a, level, __ldcg(&a.planSmall[par][it]), &ws.t.wp);
+          else plan_small_warp<U, kIdx>(a, level, __ldcg(&a.planSmall[par][it]));
         }
       }
       ++phase;

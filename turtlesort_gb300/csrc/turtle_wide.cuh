@@ -345,7 +345,7 @@ __device__ __noinline__ void plan31_item(const SortArgs& a, int pass, int item,
             push_leaf(a, pos, m, dstIsA ? 0 : 1);
           } else {
             int tb = 0, ntc = 0;
-            si = alloc_segment<kTile>(a, nextPar, pos, m, &tb, &ntc, false);
+            si = alloc_segment<kTile>(a, nextPar, pos, m, &tb, &ntc, true);
             if (si >= 0) a.segs[nextPar][si].nsamp = kWideSamples;
             sm.gTb[g] = tb;
             sm.gNt[g] = si >= 0 ? ntc : 0;
@@ -378,6 +378,112 @@ __device__ __noinline__ void plan31_item(const SortArgs& a, int pass, int item,
                          tid, kThreads);
   }
   __syncthreads();
+}
+
+// plan31_item for a segment of at most kSmallPlanTiles tiles, by one warp:
+// lane k owns class k, so the destinations of the segment's tiles are a
+// running prefix over its tiles in memory order (one 128-byte row read and
+// one 256-byte row write per tile); the warp then routes the 31 classes as
+// item 0 does.  `scratch` is the warp's own pivot slot (idle during PLAN).
+template <typename U, bool kIdx>
+__device__ __noinline__ void plan31_small_warp(const SortArgs& a, int pass, int seg,
+                                               WidePivots<typename Persist<U, kIdx>::KT>* scratch) {
+  using P = Persist<U, kIdx>;
+  using KT = typename P::KT;
+  constexpr int kTile = P::kTile, kLeafMax = P::kLeafMax;
+  const int par = pass & 1;
+  const int lane = threadIdx.x & 31;
+  SegDesc* sdp = &a.segs[par][seg];
+  const long long sdStart = __ldcg(&sdp->start);
+  const int tileBase = __ldcg(&sdp->tileBase);
+  const int nt = __ldcg(&sdp->ntiles);
+  const int* cnt = a.tileCnt[par] + (long long)tileBase * kRow;
+  long long* off = a.tileOff[par] + (long long)tileBase * kRow;
+  const int tot = lane < kWideClasses ? __ldcg(&sdp->tot[lane]) : 0;
+  int incl = tot;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(kFull, incl, o);
+    if (lane >= o) incl += y;
+  }
+  const int base = incl - tot;                   // class start relative to the segment
+  const int end = __shfl_sync(kFull, incl, 31);  // segment size
+  {
+    long long run = sdStart + base;
+#pragma unroll 4
+    for (int t = 0; t < nt; ++t) {
+      const int v = __ldcg(cnt + (long long)t * kRow + lane);
+      off[(long long)t * kRow + lane] = run;
+      run += v;
+    }
+  }
+  wide_pivots_warp<KT>(sdp, scratch);
+  const WidePivots<KT> wp = *scratch;
+  // routing: lane k = class k; child ci is classes 8ci .. 8ci+6
+  const bool dstIsA = (par == 1);
+  const int nextPar = par ^ 1;
+  const int k = lane, ci = k >> 3, jj = k & 7;
+  const int cBase = __shfl_sync(kFull, base, 8 * ci);
+  const int cEnd = __shfl_sync(kFull, base, 8 * ci + 7);  // start of class 8ci+7
+  unsigned park = 0u;
+  int si = -1, tb = 0, ntc = 0;
+  const long long pos = sdStart + base;
+  const long long m = tot;
+  if (k < kWideClasses) {
+    const long long cStart = sdStart + cBase;
+    const long long cN = (long long)cEnd - cBase;
+    const bool leafChild = cN <= kLeafMax;
+    if (jj == 7) {  // the parent's pivot run ci
+      if (m > 0 && !dstIsA) {
+        push_fill(a, pos, m, (unsigned long long)wp.par.p[ci]);
+        park = 1u;
+      }
+    } else if (leafChild) {
+      if (jj == 0 && (cN > 1 || (cN == 1 && !dstIsA))) push_leaf(a, cStart, cN, dstIsA ? 0 : 1);
+    } else if (jj & 1) {  // child ci's pivot run jj/2
+      if (m > 0 && !dstIsA) {
+        push_fill(a, pos, m, (unsigned long long)wp.child[ci].p[jj >> 1]);
+        park = 1u;
+      }
+    } else if (m > 1 || (m == 1 && !dstIsA)) {  // grandchild
+      if (m <= kLeafMax) {
+        push_leaf(a, pos, m, dstIsA ? 0 : 1);
+      } else {
+        si = alloc_segment<kTile>(a, nextPar, pos, m, &tb, &ntc, true);
+        if (si >= 0) a.segs[nextPar][si].nsamp = kWideSamples;
+      }
+    }
+    sdp->cbase[k] = pos;
+  } else {
+    sdp->cbase[31] = sdStart + end;
+  }
+  const unsigned pm = __ballot_sync(kFull, park != 0u);
+  // tiles of the new segments; grandchild g = 4ci + q is class 8ci + 2q
+  int gseg = -1;
+#pragma unroll
+  for (int g = 0; g < 16; ++g) {
+    const int src = 8 * (g >> 2) + 2 * (g & 3);
+    const int s = __shfl_sync(kFull, si, src);
+    if (lane == g) gseg = s;
+    if (s >= 0) {
+      const int ctb = __shfl_sync(kFull, tb, src);
+      const int cnt2 = __shfl_sync(kFull, ntc, src);
+      const long long cs = __shfl_sync(kFull, pos, src);
+      const long long cn = __shfl_sync(kFull, m, src);
+      write_tiles<kTile>(a, nextPar, s, ctb, cnt2, cs, cn, lane, 32);
+    }
+  }
+  if (lane < 16) sdp->childSeg[lane] = gseg;
+  if (lane == 0) {
+    sdp->parkMask = pm;
+    for (int q = 0; q < 3; ++q) sdp->pivS[q] = (unsigned long long)wp.par.p[q];
+    sdp->lut = wp.par.lut;
+    for (int c = 0; c < 4; ++c) {
+      for (int q = 0; q < 3; ++q) sdp->cpiv[c][q] = (unsigned long long)wp.child[c].p[q];
+      sdp->clut[c] = wp.child[c].lut;
+    }
+  }
+  __syncwarp();
 }
 
 // SCATTER of a two-level pass: scatter_tile_warp with 31 classes.  Lane
@@ -449,56 +555,59 @@ __device__ __forceinline__ void scatter31_tile_warp(const SortArgs& a, int pass,
   U* dstK = (U*)(par ? a.keysA : a.keysB);
   int* dstI = par ? a.idxA : a.idxB;
 
+  unsigned lt;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
   for (int ch = chBeg; ch < chEnd; ++ch) {
     const int b = (ch - chBeg) & 1;
     const long long c0 = abs0 + (long long)ch * kWCH;
     if (ch + 1 < chEnd && lane == 0 && chunk_bulk_ok<U, kIdx>(srcK, srcI, c0 + kWCH, a.n))
       chunk_bulk_issue<U, kIdx, true>(ws, b ^ 1, srcK, srcI, c0 + kWCH);
-    const int e0 = ch * kWCH + lane * kItems;
+    // lane-strided items: item i of this lane is chunk element 32 * i + lane,
+    // so ranking item by item follows memory order (stable)
+    const bool inner = ch * kWCH >= rlo && (ch + 1) * kWCH <= rhi;
     KT key[kItems];
-    // keys of the lane inside the tile (every key of an interior chunk)
-    unsigned okm = (1u << kItems) - 1u;
-    if (ch * kWCH < rlo || (ch + 1) * kWCH > rhi) {
-      okm = 0;
-#pragma unroll
-      for (int i = 0; i < kItems; ++i) okm |= (e0 + i >= rlo && e0 + i < rhi) ? (1u << i) : 0u;
-    }
     if (chunk_bulk_ok<U, kIdx>(srcK, srcI, c0, a.n)) {
       chunk_wait<U, kIdx>(ws, b, phases, a.ctrl);
-      chunk_keys<U, kIdx>(ws, b, lane, flip, key);
-    } else {
-      load_chunk<U, KT, kItems>(srcK + abs0, abs0, a.n, e0, rlo, rhi, flip, key);
-      if (kIdx) {
-        int id[kItems];
-        load_ids<kItems>(srcI + abs0, abs0, a.n, e0, okm, id);
 #pragma unroll
-        for (int i = 0; i < kItems; ++i) ws.pi[b][lane * kItems + i] = id[i];
+      for (int i = 0; i < kItems; ++i) key[i] = KT(ws.pk[b][32 * i + lane]) ^ flip;
+    } else {
+      // array end: plain loads; the ids go through the buffer like bulk ones
+#pragma unroll
+      for (int i = 0; i < kItems; ++i) {
+        const int e = ch * kWCH + 32 * i + lane;
+        const bool ok = e >= rlo && e < rhi;
+        key[i] = ok ? KT(__ldcg(srcK + abs0 + e)) ^ flip : KT(0);
+        if (kIdx) ws.pi[b][32 * i + lane] = ok ? __ldcg(srcI + abs0 + e) : 0;
       }
     }
-    // classes (5 bits each, 31 = no key) and in-lane ranks (4 bits each)
-    unsigned cwLo = 0, cwHi = 0, rw = 0;
-    unsigned acc4[4] = {0u, 0u, 0u, 0u};
+    ws.t.cnt[lane] = 0;
+    __syncwarp();
+    // class (5 bits, 31 = no key) and rank in the chunk (8 bits) of each item
+    unsigned cwLo = 0, cwHi = 0, rk0 = 0, rk1 = 0;
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
-      unsigned k = 31u;
-      if (okm >> i & 1u) {
-        k = wide_class_of<KT>(key[i], pp, child);
-        const unsigned w = k >> 3;
-        const unsigned x = w == 0u ? acc4[0] : w == 1u ? acc4[1] : w == 2u ? acc4[2] : acc4[3];
-        rw |= ((x >> (4u * (k & 7u))) & 15u) << (4 * i);
-        wide_bump(acc4, k);
+      const int e = ch * kWCH + 32 * i + lane;
+      const unsigned k = (inner || (e >= rlo && e < rhi)) ? wide_class_of<KT>(key[i], pp, child)
+                                                          : 31u;
+      // lanes of the same class: one vote per class bit
+      unsigned peers = 0xffffffffu;
+#pragma unroll
+      for (int bit = 0; bit < 5; ++bit) {
+        const unsigned m = __ballot_sync(kFull, (k >> bit) & 1u);
+        peers &= ((k >> bit) & 1u) ? m : ~m;
       }
+      const int base = ws.t.cnt[k];
+      const unsigned r = (unsigned)(base + __popc(peers & lt));
+      __syncwarp();
+      if ((peers >> lane) == 1u) ws.t.cnt[k] = base + __popc(peers);  // highest lane of the class
+      __syncwarp();
+      if (i < 4) rk0 |= r << (8 * i);
+      else rk1 |= r << (8 * (i - 4));
       if (i < 6) cwLo |= k << (5 * i);
       else cwHi |= k << (5 * (i - 6));
     }
-    // eight words of 8-bit fields (classes 4w..4w+3)
-    unsigned a8[8];
-#pragma unroll
-    for (int w = 0; w < 4; ++w) {
-      a8[2 * w] = widen_lo(acc4[w]);
-      a8[2 * w + 1] = widen_hi(acc4[w]);
-    }
-    const int totk = wide_totals(a8);  // lane k: chunk total of class k
+    // class starts in the stage (lane k: class k; class 31 holds no key)
+    const int totk = lane < kWideClasses ? ws.t.cnt[lane] : 0;
     int csk = totk;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -506,23 +615,8 @@ __device__ __forceinline__ void scatter31_tile_warp(const SortArgs& a, int pass,
       if (lane >= o) csk += y;
     }
     const int nv = __shfl_sync(kFull, csk, 31);
-    csk -= totk;  // lane k: start of class k in the stage
-    // stage slot words: the class starts of classes 4w..4w+3 plus the lane's
-    // exclusive prefix within each class (warp scan of packed 8-bit fields;
-    // exclusive sums stay below 256, so the packed arithmetic is exact)
-    const unsigned mineCs = (unsigned)csk << (8 * (lane & 3));
-    unsigned grp = mineCs + __shfl_xor_sync(kFull, mineCs, 1);
-    grp += __shfl_xor_sync(kFull, grp, 2);
-#pragma unroll
-    for (int w = 0; w < 8; ++w) {
-      unsigned s = a8[w];
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const unsigned y = __shfl_up_sync(kFull, s, o);
-        if (lane >= o) s += y;
-      }
-      ws.t.bword[w][lane] = __shfl_sync(kFull, grp, 4 * w) + (s - a8[w]);
-    }
+    csk -= totk;
+    ws.t.cs[lane] = csk;
     // destination table of the chunk: delta[k] = running base - class start
     const long long wbLo = ws.t.wbase[lane];
     ws.t.delta[lane] = wbLo - (long long)csk;
@@ -530,21 +624,13 @@ __device__ __forceinline__ void scatter31_tile_warp(const SortArgs& a, int pass,
     __syncwarp();
     // stage by class
 #pragma unroll
-    for (int h = 0; h < kItems; h += 4) {
-      int4 idv = make_int4(0, 0, 0, 0);
-      if (kIdx) idv = *reinterpret_cast<const int4*>(&ws.pi[b][lane * kItems + h]);
-      const int idq[4] = {idv.x, idv.y, idv.z, idv.w};
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int i = h + u;
-        const unsigned k = i < 6 ? (cwLo >> (5 * i)) & 31u : (cwHi >> (5 * (i - 6))) & 31u;
-        if (k != 31u) {
-          const unsigned pos =
-              ((ws.t.bword[k >> 2][lane] >> (8u * (k & 3u))) & 0xFFu) + ((rw >> (4 * i)) & 15u);
-          ws.sk[pos] = key[i];
-          if (kIdx) ws.si[pos] = idq[u];
-          ws.sc[pos] = (unsigned char)k;
-        }
+    for (int i = 0; i < kItems; ++i) {
+      const unsigned k = i < 6 ? (cwLo >> (5 * i)) & 31u : (cwHi >> (5 * (i - 6))) & 31u;
+      if (k != 31u) {
+        const unsigned pos = (unsigned)ws.t.cs[k] + ((i < 4 ? rk0 >> (8 * i) : rk1 >> (8 * (i - 4))) & 0xFFu);
+        ws.sk[pos] = key[i];
+        if (kIdx) ws.si[pos] = ws.pi[b][32 * i + lane];
+        ws.sc[pos] = (unsigned char)k;
       }
     }
     __syncwarp();
