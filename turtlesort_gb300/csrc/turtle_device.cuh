@@ -146,6 +146,7 @@ struct Control {
   unsigned long long segTile[2];  // packed (segments << 32 | tiles) per level parity
   int planCount[2];               // plan items per level parity
   int planSmallCount[2];          // small segments (one warp plans each) per level parity
+  int planMulti[2];               // 1: some segment of the level has several plan items
   unsigned int smallWork;         // small-segment plan counter of the current level
   int leafCount;
   int fillCount;
@@ -191,7 +192,9 @@ struct SortArgs {
   long long* tileOff[2];     // [tile][kRow] global destination of each class
   int* planSmall[2];         // one-level passes: segments of at most kSmallPlanTiles tiles,
                              // each planned by one warp
-  int* planSeg[2];           // segment of each plan item (kPartTile * kThreads keys)
+  int* planSeg[2];           // segment of each plan item
+  int* itemTot[2];           // [item][kRow] column sums of each plan item's count rows
+  unsigned char* cls;        // two-level passes: class of each key, written by COUNT for SCATTER (kPartTile * kThreads keys)
   LeafDesc* leaves;
   LeafDesc* leavesSorted;
   FillDesc* fills;

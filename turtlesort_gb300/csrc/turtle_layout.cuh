@@ -14,13 +14,18 @@ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 struct WsLayout {
   int segCap = 0, tileCap = 0, leafCap = 0, fillCap = 0, planCap = 0;
-  size_t offPlanSeg[2] = {0, 0}, offPlanSmall[2] = {0, 0};
+  size_t offPlanSeg[2] = {0, 0}, offPlanSmall[2] = {0, 0}, offItemTot[2] = {0, 0};
   size_t offCtrl = 0, offSegs[2] = {0, 0}, offTiles[2] = {0, 0}, offTileCnt[2] = {0, 0},
          offTileOff[2] = {0, 0};
   size_t offLeaves = 0, offLeavesSorted = 0, offFills = 0, bytes = 0;
+  bool hasCls = false;   // per-key class bytes (two-level passes need them)
+  size_t offCls = 0;
 };
 
-inline WsLayout make_layout(long long maxN, int tile, int leafMax, long long extraLeaves) {
+// classBytes: room for the per-key class bytes of two-level passes (without
+// it, sorts use one-level passes only).
+inline WsLayout make_layout(long long maxN, int tile, int leafMax, long long extraLeaves,
+                            bool classBytes = true) {
   WsLayout L;
   // segments of one level are disjoint and longer than leafMax
   const long long segCap = maxN / leafMax + 66;
@@ -45,9 +50,11 @@ inline WsLayout make_layout(long long maxN, int tile, int leafMax, long long ext
   for (int p = 0; p < 2; ++p) { L.offTileOff[p] = o; o = align_up(o + tileCap * turtle::kRow * sizeof(long long), 256); }
   for (int p = 0; p < 2; ++p) { L.offPlanSeg[p] = o; o = align_up(o + planCap * sizeof(int), 256); }
   for (int p = 0; p < 2; ++p) { L.offPlanSmall[p] = o; o = align_up(o + segCap * sizeof(int), 256); }
+  for (int p = 0; p < 2; ++p) { L.offItemTot[p] = o; o = align_up(o + planCap * turtle::kRow * sizeof(int), 256); }
   L.offLeaves = o; o = align_up(o + leafCap * sizeof(turtle::LeafDesc), 256);
   L.offLeavesSorted = o; o = align_up(o + leafCap * sizeof(turtle::LeafDesc), 256);
   L.offFills = o; o = align_up(o + fillCap * sizeof(turtle::FillDesc), 256);
+  if (classBytes) { L.hasCls = true; L.offCls = o; o = align_up(o + (size_t)maxN + 16, 256); }
   L.bytes = o;
   return L;
 }
@@ -115,6 +122,7 @@ inline SortArgs bind_args(void* keys, int* idx, void* keysB, int* idxB, char* ws
     a.tileOff[p] = (long long*)(ws + L.offTileOff[p]);
     a.planSeg[p] = (int*)(ws + L.offPlanSeg[p]);
     a.planSmall[p] = (int*)(ws + L.offPlanSmall[p]);
+    a.itemTot[p] = (int*)(ws + L.offItemTot[p]);
   }
   a.leaves = (LeafDesc*)(ws + L.offLeaves);
   a.leavesSorted = (LeafDesc*)(ws + L.offLeavesSorted);
@@ -126,6 +134,8 @@ inline SortArgs bind_args(void* keys, int* idx, void* keysB, int* idxB, char* ws
   a.planCap = L.planCap;
   a.ctrl = (Control*)(ws + L.offCtrl);
   if (rule == kRuleAuto) rule = n >= kAutoTwoLevelKeys ? kRuleTwoLevel : kRuleSampled;
+  if (rule == kRuleTwoLevel && !L.hasCls) rule = kRuleSampled;
+  a.cls = L.hasCls ? (unsigned char*)(ws + L.offCls) : nullptr;
   a.samples = rule_samples(rule);
   a.slices = 1;
   a.leafYield = 0;

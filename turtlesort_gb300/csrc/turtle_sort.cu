@@ -85,6 +85,7 @@ struct Persist {
     KT sk[kWCH];                    // staged keys (class order)
     int si[kIdx ? kWCH : 4];        // staged ids
     unsigned char sc[kWCH];         // class of each stage slot
+    alignas(16) unsigned char pc[2][kWCH];  // two-level SCATTER: class bytes of the chunks in flight
     struct OneLevel {               // tables of a one-level pass (7 classes)
       long long delta[8];           // destination minus stage slot, per class
       long long wbase[8];           // running destination per class
@@ -121,7 +122,6 @@ struct Persist {
   struct Smem {  // partition CTA
     WarpArea w[kWarps];
     int red[kWarps][8];
-    int redPre[kWarps][8];
     int pre[8];
     int tot[8];
     int cbase[8];                   // class boundaries relative to the segment start
@@ -130,6 +130,8 @@ struct Persist {
     long long childStart[4], childN[4];
     KT piv[3];
     unsigned lut;
+    int rowSum[kWarps][kRow];       // plan item totals: per-warp column sums
+    int preAll[kRow];               // column sums of the item's segment before the item
     int classOff[kMaxSlices * 16];  // leaf buckets: (slice, size class)
     int classItems[kMaxSlices * 16];
     // two-level plan
@@ -296,6 +298,7 @@ __device__ int alloc_segment(const SortArgs& a, int par, long long start, long l
     return -1;
   }
   if (small) a.planSmall[par][pb] = si;
+  if (np > 1) a.ctrl->planMulti[par] = 1;  // the plan sums per-item totals first
   // only the fields read before the plan writes them: the samples come from
   // the parent's scatter, pivots, class bases and children from the plan
   SegDesc* d = &a.segs[par][si];
@@ -596,6 +599,56 @@ __device__ __forceinline__ void count_tile_warp(const SortArgs& a, int level, in
 // PLAN phase: one plan item per CTA
 // ---------------------------------------------------------------------------
 
+// PLAN, first step (levels with segments of several plan items): the column
+// sums of one item's count rows (warp w sums rows w, w + kWarps, ...; lane =
+// column), so that the plan of a later item of the segment reads the totals
+// of the items before it instead of all their rows.
+template <typename U, bool kIdx>
+__device__ __noinline__ void item_totals(const SortArgs& a, int level, int item,
+                                         typename Persist<U, kIdx>::Smem& sm) {
+  const int par = level & 1;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int seg = __ldcg(&a.planSeg[par][item]);
+  const SegDesc* sdp = &a.segs[par][seg];
+  const int j = item - __ldcg(&sdp->planBase);
+  const int tileBase = __ldcg(&sdp->tileBase), nt = __ldcg(&sdp->ntiles);
+  const int t0 = j * kThreads, t1 = nt < t0 + kThreads ? nt : t0 + kThreads;
+  const int* cnt = a.tileCnt[par] + (long long)tileBase * kRow;
+  int acc = 0;
+#pragma unroll 8
+  for (int t = t0 + warp; t < t1; t += kWarps) acc += __ldcg(cnt + (long long)t * kRow + lane);
+  sm.rowSum[warp][lane] = acc;
+  __syncthreads();
+  if (tid < kRow) {
+    int s = 0;
+    for (int w = 0; w < kWarps; ++w) s += sm.rowSum[w][tid];
+    a.itemTot[par][(long long)item * kRow + tid] = s;
+  }
+  __syncthreads();
+}
+
+// Column sums of the items of a segment before item j (threads 0..kRow-1),
+// into sm.preAll.  The caller synchronizes.
+template <typename U, bool kIdx>
+__device__ __forceinline__ void item_prefix(const SortArgs& a, int par, int planBase, int j,
+                                            typename Persist<U, kIdx>::Smem& sm) {
+  const int tid = threadIdx.x;
+  if (tid < kRow) {
+    // independent loads, several in flight (the chain of adds is cheap)
+    const int* col = a.itemTot[par] + (long long)planBase * kRow + tid;
+    int s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+    int i = 0;
+    for (; i + 4 <= j; i += 4) {
+      s0 += __ldcg(col + (long long)i * kRow);
+      s1 += __ldcg(col + (long long)(i + 1) * kRow);
+      s2 += __ldcg(col + (long long)(i + 2) * kRow);
+      s3 += __ldcg(col + (long long)(i + 3) * kRow);
+    }
+    for (; i < j; ++i) s0 += __ldcg(col + (long long)i * kRow);
+    sm.preAll[tid] = s0 + s1 + s2 + s3;
+  }
+}
+
 // One plan item: kThreads consecutive tiles (item j of segment `seg`, one
 // tile per thread).  The class bases of the segment follow from its class
 // totals (summed by COUNT) in class order as in turtle-sort.cu:755-761; the
@@ -615,13 +668,17 @@ __device__ __noinline__ void plan_item(const SortArgs& a, int level, int item,
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int seg = __ldcg(&a.planSeg[par][item]);
   SegDesc* sdp = &a.segs[par][seg];
-  const int j = item - __ldcg(&sdp->planBase);
+  const int planBase = __ldcg(&sdp->planBase);
+  const int j = item - planBase;
   const long long sdStart = __ldcg(&sdp->start);
   const int tileBase = __ldcg(&sdp->tileBase);
   const int nt = __ldcg(&sdp->ntiles);
   const int* cnt = a.tileCnt[par] + (long long)tileBase * kRow;
   const int t0 = j * kThreads;
   if (tid < 7) sm.tot[tid] = __ldcg(&sdp->tot[tid]);
+  // the segment's tiles before this item: their raw predicate totals (the
+  // class map is additive over tiles) from the item totals
+  item_prefix<U, kIdx>(a, par, planBase, j, sm);
   if (j == 0 && warp == 0) {
     KT piv[3];
     segment_pivots_warp<KT, U>(sdp, (const U*)(par ? a.keysB : a.keysA), level, (KT)a.flip,
@@ -631,22 +688,8 @@ __device__ __noinline__ void plan_item(const SortArgs& a, int level, int item,
       sm.lut = pivot_lut(piv[0] == piv[1], piv[1] == piv[2]);
     }
   }
-  // counts of the segment's tiles before this item, and of this thread's tile
-  // (the class map is additive over tiles: sum the raw predicate rows, then
-  // convert once)
-  int pre[7], v[7];
-  {
-    int4 r0 = make_int4(0, 0, 0, 0), r1 = make_int4(0, 0, 0, 0);
-#pragma unroll 8
-    for (int t = tid; t < t0; t += kThreads) {
-      const int4* row = reinterpret_cast<const int4*>(cnt + (long long)t * kRow);
-      const int4 x = __ldcg(row), y = __ldcg(row + 1);
-      r0.x += x.x; r0.y += x.y; r0.z += x.z; r0.w += x.w;
-      r1.x += y.x; r1.y += y.y; r1.z += y.z;
-    }
-    const int pc[6] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y};
-    classes_from_predicates(pc, r1.z, pre);
-  }
+  // counts of this thread's tile
+  int v[7];
 #pragma unroll
   for (int c = 0; c < 7; ++c) v[c] = 0;
   const int myTile = t0 + tid;
@@ -654,7 +697,6 @@ __device__ __noinline__ void plan_item(const SortArgs& a, int level, int item,
   int inc[7];
 #pragma unroll
   for (int c = 0; c < 7; ++c) {
-    const int ps = (int)__reduce_add_sync(kFull, (unsigned)pre[c]);
     int x = v[c];
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -662,18 +704,23 @@ __device__ __noinline__ void plan_item(const SortArgs& a, int level, int item,
       if (lane >= o) x += y;
     }
     inc[c] = x;
-    if (lane == 31) { sm.red[warp][c] = x; sm.redPre[warp][c] = ps; }
+    if (lane == 31) sm.red[warp][c] = x;
   }
   __syncthreads();
   if (tid < 7) {
-    int acc = 0, pacc = 0;
+    int acc = 0;
     for (int w = 0; w < kWarps; ++w) {
       const int x = sm.red[w][tid];
       sm.red[w][tid] = acc;
       acc += x;
-      pacc += sm.redPre[w][tid];
     }
-    sm.pre[tid] = pacc;
+  }
+  if (tid == 7) {
+    int pre[7];
+    const int pc[6] = {sm.preAll[0], sm.preAll[1], sm.preAll[2], sm.preAll[3], sm.preAll[4],
+                       sm.preAll[5]};
+    classes_from_predicates(pc, sm.preAll[6], pre);
+    for (int c = 0; c < 7; ++c) sm.pre[c] = pre[c];
   }
   if (tid == 0) {
     int b = 0;
@@ -1227,6 +1274,19 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
     if (!grid_barrier(c)) return;
     timeline_mark(c, ntiles);
 
+    // PLAN, first step when a segment has several plan items: item totals
+    if (ld_acquire_int(&c->planMulti[par])) {
+      unsigned* wc = &c->work[phase & 3];
+      if (blockIdx.x == 0 && tid == 0) c->work[(phase + 2) & 3] = 0;
+      for (;;) {
+        const int it = claim_item(wc);
+        if (it >= nplan) break;
+        item_totals<U, kIdx>(a, level, it, sm);
+      }
+      ++phase;
+      __threadfence();
+      if (!grid_barrier(c)) return;
+    }
     // PLAN: one item (kThreads tiles of one segment) per CTA
     {
       unsigned* wc = &c->work[phase & 3];
@@ -1262,6 +1322,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
       st.store(0ull, cuda::memory_order_relaxed);
       c->planCount[par] = 0;
       c->planSmallCount[par] = 0;
+      c->planMulti[par] = 0;
       c->smallWork = 0;
       c->work[(phase + 2) & 3] = 0;
     }

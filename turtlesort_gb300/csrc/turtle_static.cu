@@ -56,7 +56,7 @@ struct Plan {
 Plan plan_for(int width) {
   Plan p;
   p.lay = turtle::make_layout(kStaticMaxElements, turtle::kernels_tile_elems(width),
-                              turtle::kernels_leaf_max(width), 0);
+                              turtle::kernels_leaf_max(width), 0, false);
   p.offIdx = turtle::align_up((size_t)kStaticMaxElements * width, 256);
   p.offWs = turtle::align_up(p.offIdx + (size_t)kStaticMaxElements * sizeof(int32_t), 256);
   p.bytes = p.offWs + p.lay.bytes;

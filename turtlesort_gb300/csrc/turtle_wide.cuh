@@ -144,8 +144,9 @@ __device__ __forceinline__ int wide_totals(const unsigned* a8) {
 }
 
 // COUNT of a two-level pass: tile t's 31 class counts go to its row of
-// tileCnt; the warp's running class totals of the segment (accSeg / accCnt,
-// lane k holds class k) go to the segment when the warp moves on.
+// tileCnt and each key's class to its byte of a.cls (for SCATTER); the warp's
+// running class totals of the segment (accSeg / accCnt, lane k holds class k)
+// go to the segment when the warp moves on.
 template <typename U, bool kIdx>
 __device__ __forceinline__ void count31_tile_warp(const SortArgs& a, int pass, int t,
                                                   typename Persist<U, kIdx>::WarpArea& ws,
@@ -194,9 +195,27 @@ __device__ __forceinline__ void count31_tile_warp(const SortArgs& a, int pass, i
       load_chunk<U, KT, kItems>(src + abs0, abs0, a.n, e0, rlo, rhi, flip, key);
     }
     unsigned acc4[4] = {0u, 0u, 0u, 0u};
+    unsigned cb0 = 0, cb1 = 0;  // the keys' classes, one byte each, for SCATTER
 #pragma unroll
-    for (int i = 0; i < kItems; ++i)
-      if (okm >> i & 1u) wide_bump(acc4, wide_class_of<KT>(key[i], pp, child));
+    for (int i = 0; i < kItems; ++i) {
+      if (okm >> i & 1u) {
+        const unsigned k = wide_class_of<KT>(key[i], pp, child);
+        wide_bump(acc4, k);
+        if (i < 4) cb0 |= k << (8 * i);
+        else cb1 |= k << (8 * (i - 4));
+      }
+    }
+    {
+      unsigned char* cdst = a.cls + c0 + lane * kItems;
+      if (okm == (1u << kItems) - 1u) {
+        if (kItems == 8) *reinterpret_cast<uint2*>(cdst) = make_uint2(cb0, cb1);
+        else *reinterpret_cast<unsigned*>(cdst) = cb0;
+      } else {
+#pragma unroll
+        for (int i = 0; i < kItems; ++i)
+          if (okm >> i & 1u) cdst[i] = (unsigned char)((i < 4 ? cb0 >> (8 * i) : cb1 >> (8 * (i - 4))) & 0xFFu);
+      }
+    }
 #pragma unroll
     for (int w = 0; w < 4; ++w) {
       acc8[2 * w] += widen_lo(acc4[w]);
@@ -233,13 +252,16 @@ __device__ __noinline__ void plan31_item(const SortArgs& a, int pass, int item,
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int seg = __ldcg(&a.planSeg[par][item]);
   SegDesc* sdp = &a.segs[par][seg];
-  const int j = item - __ldcg(&sdp->planBase);
+  const int planBase = __ldcg(&sdp->planBase);
+  const int j = item - planBase;
   const long long sdStart = __ldcg(&sdp->start);
   const int tileBase = __ldcg(&sdp->tileBase);
   const int nt = __ldcg(&sdp->ntiles);
   const int* cnt = a.tileCnt[par] + (long long)tileBase * kRow;
   const int t0 = j * kThreads;
   const int myTile = t0 + tid;
+  // class counts of the segment's tiles before this item, from the item totals
+  item_prefix<U, kIdx>(a, par, planBase, j, sm);
   if (tid < 32) {
     int x = tid < kWideClasses ? __ldcg(&sdp->tot[tid]) : 0;
     const int tot = x;
@@ -254,16 +276,9 @@ __device__ __noinline__ void plan31_item(const SortArgs& a, int pass, int item,
   if (j == 0 && warp == 1) wide_pivots_warp<KT>(sdp, &sm.wpiv);
   // offsets, eight classes per round
   for (int g = 0; g < 4; ++g) {
-    int pre[8], v[8], inc[8];
+    int v[8], inc[8];
 #pragma unroll
-    for (int c = 0; c < 8; ++c) { pre[c] = 0; v[c] = 0; }
-#pragma unroll 4
-    for (int t = tid; t < t0; t += kThreads) {
-      const int4* row = reinterpret_cast<const int4*>(cnt + (long long)t * kRow + 8 * g);
-      const int4 x = __ldcg(row), y = __ldcg(row + 1);
-      pre[0] += x.x; pre[1] += x.y; pre[2] += x.z; pre[3] += x.w;
-      pre[4] += y.x; pre[5] += y.y; pre[6] += y.z; pre[7] += y.w;
-    }
+    for (int c = 0; c < 8; ++c) v[c] = 0;
     if (myTile < nt) {
       const int4* row = reinterpret_cast<const int4*>(cnt + (long long)myTile * kRow + 8 * g);
       const int4 x = __ldcg(row), y = __ldcg(row + 1);
@@ -272,7 +287,6 @@ __device__ __noinline__ void plan31_item(const SortArgs& a, int pass, int item,
     }
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
-      const int ps = (int)__reduce_add_sync(kFull, (unsigned)pre[c]);
       int x = v[c];
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
@@ -280,18 +294,17 @@ __device__ __noinline__ void plan31_item(const SortArgs& a, int pass, int item,
         if (lane >= o) x += y;
       }
       inc[c] = x;
-      if (lane == 31) { sm.red[warp][c] = x; sm.redPre[warp][c] = ps; }
+      if (lane == 31) sm.red[warp][c] = x;
     }
     __syncthreads();
     if (tid < 8) {
-      int acc = 0, pacc = 0;
+      int acc = 0;
       for (int w = 0; w < kWarps; ++w) {
         const int x = sm.red[w][tid];
         sm.red[w][tid] = acc;
         acc += x;
-        pacc += sm.redPre[w][tid];
       }
-      sm.pre[tid] = pacc;
+      sm.pre[tid] = sm.preAll[8 * g + tid];
     }
     __syncthreads();
     if (myTile < nt) {
@@ -486,13 +499,28 @@ __device__ __noinline__ void plan31_small_warp(const SortArgs& a, int pass, int 
   __syncwarp();
 }
 
-// SCATTER of a two-level pass: scatter_tile_warp with 31 classes.  Lane
-// counts are 4-bit fields of four words (word = child), the warp scan runs on
-// eight words of 8-bit fields, the class starts come from a lane scan of the
-// class totals, and each lane's stage slots per class (8-bit fields of eight
-// words) sit in shared memory.  Lane k also watches the sample positions of
-// grandchild class k and copies the staged key written there into the new
-// segment's samples.
+// Lane 0: bulk-copy keys, ids and class bytes of the chunk at c0 into buffer b.
+template <typename U, bool kIdx>
+__device__ __forceinline__ void wide_bulk_issue(typename Persist<U, kIdx>::WarpArea& ws, int b,
+                                                const U* srcK, const int* srcI,
+                                                const unsigned char* cls, long long c0) {
+  constexpr int kWCH = Persist<U, kIdx>::kWCH;
+  constexpr unsigned kBytes = kWCH * sizeof(U) + (kIdx ? kWCH * 4 : 0) + kWCH;
+  fence_proxy_async_smem();
+  mbar_arm(&ws.mbar[b], kBytes);
+  bulk_g2s(ws.pk[b], srcK + c0, kWCH * sizeof(U), &ws.mbar[b]);
+  if (kIdx) bulk_g2s(ws.pi[b], srcI + c0, kWCH * 4, &ws.mbar[b]);
+  bulk_g2s(ws.pc[b], cls + c0, kWCH, &ws.mbar[b]);
+}
+
+// SCATTER of a two-level pass: scatter_tile_warp with 31 classes.  The keys'
+// classes come from COUNT (one byte per key, bulk-copied with the keys and
+// ids).  Items are lane-strided (item i of lane l is chunk element 32i + l),
+// so ranking them item by item keeps memory order: the lanes of one class
+// are found with one vote per class bit, and a per-warp running count per
+// class gives the rank.  The class starts come from a lane scan of the chunk's
+// class totals.  Lane k also watches the sample positions of grandchild class
+// k and copies the staged key written there into the new segment's samples.
 template <typename U, bool kIdx>
 __device__ __forceinline__ void scatter31_tile_warp(const SortArgs& a, int pass, int t,
                                                     typename Persist<U, kIdx>::WarpArea& ws,
@@ -510,21 +538,8 @@ __device__ __forceinline__ void scatter31_tile_warp(const SortArgs& a, int pass,
   const int* srcI = par ? a.idxB : a.idxA;
   const int chBeg = rlo / kWCH, chEnd = (rhi + kWCH - 1) / kWCH;
   if (lane == 0 && chunk_bulk_ok<U, kIdx>(srcK, srcI, abs0 + (long long)chBeg * kWCH, a.n))
-    chunk_bulk_issue<U, kIdx, true>(ws, 0, srcK, srcI, abs0 + (long long)chBeg * kWCH);
+    wide_bulk_issue<U, kIdx>(ws, 0, srcK, srcI, a.cls, abs0 + (long long)chBeg * kWCH);
   const SegDesc* sdp = &a.segs[par][td.seg];
-  if (td.seg != ws.t.pivSeg) {
-    if (lane == 0) {
-      WidePivots<KT> wp;
-      for (int q = 0; q < 3; ++q) wp.par.p[q] = (KT)__ldcg(&sdp->pivS[q]);
-      wp.par.lut = __ldcg(&sdp->lut);
-      for (int c = 0; c < 4; ++c) {
-        for (int q = 0; q < 3; ++q) wp.child[c].p[q] = (KT)__ldcg(&sdp->cpiv[c][q]);
-        wp.child[c].lut = __ldcg(&sdp->clut[c]);
-      }
-      ws.t.wp = wp;
-    }
-    ws.t.pivSeg = td.seg;
-  }
   const unsigned parkMask = __ldcg(&sdp->parkMask);
   {
     // running destination of class `lane`, and its next sample position
@@ -549,9 +564,6 @@ __device__ __forceinline__ void scatter31_tile_warp(const SortArgs& a, int pass,
     ws.t.capI[lane] = nextI;
   }
   __syncwarp();
-  __syncwarp();
-  const PivotSet<KT> pp = ws.t.wp.par;
-  const PivotSet<KT>* child = ws.t.wp.child;
   U* dstK = (U*)(par ? a.keysA : a.keysB);
   int* dstI = par ? a.idxA : a.idxB;
 
@@ -561,7 +573,7 @@ __device__ __forceinline__ void scatter31_tile_warp(const SortArgs& a, int pass,
     const int b = (ch - chBeg) & 1;
     const long long c0 = abs0 + (long long)ch * kWCH;
     if (ch + 1 < chEnd && lane == 0 && chunk_bulk_ok<U, kIdx>(srcK, srcI, c0 + kWCH, a.n))
-      chunk_bulk_issue<U, kIdx, true>(ws, b ^ 1, srcK, srcI, c0 + kWCH);
+      wide_bulk_issue<U, kIdx>(ws, b ^ 1, srcK, srcI, a.cls, c0 + kWCH);
     // lane-strided items: item i of this lane is chunk element 32 * i + lane,
     // so ranking item by item follows memory order (stable)
     const bool inner = ch * kWCH >= rlo && (ch + 1) * kWCH <= rhi;
@@ -571,14 +583,16 @@ __device__ __forceinline__ void scatter31_tile_warp(const SortArgs& a, int pass,
 #pragma unroll
       for (int i = 0; i < kItems; ++i) key[i] = KT(ws.pk[b][32 * i + lane]) ^ flip;
     } else {
-      // array end: plain loads; the ids go through the buffer like bulk ones
+      // array end: plain loads; ids and classes go through the buffers like bulk ones
 #pragma unroll
       for (int i = 0; i < kItems; ++i) {
         const int e = ch * kWCH + 32 * i + lane;
         const bool ok = e >= rlo && e < rhi;
         key[i] = ok ? KT(__ldcg(srcK + abs0 + e)) ^ flip : KT(0);
         if (kIdx) ws.pi[b][32 * i + lane] = ok ? __ldcg(srcI + abs0 + e) : 0;
+        ws.pc[b][32 * i + lane] = ok ? __ldcg(a.cls + abs0 + e) : (unsigned char)31;
       }
+      __syncwarp();
     }
     ws.t.cnt[lane] = 0;
     __syncwarp();
@@ -587,8 +601,7 @@ __device__ __forceinline__ void scatter31_tile_warp(const SortArgs& a, int pass,
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
       const int e = ch * kWCH + 32 * i + lane;
-      const unsigned k = (inner || (e >= rlo && e < rhi)) ? wide_class_of<KT>(key[i], pp, child)
-                                                          : 31u;
+      const unsigned k = (inner || (e >= rlo && e < rhi)) ? (unsigned)ws.pc[b][32 * i + lane] : 31u;
       // lanes of the same class: one vote per class bit
       unsigned peers = 0xffffffffu;
 #pragma unroll
