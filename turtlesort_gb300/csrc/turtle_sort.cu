@@ -100,6 +100,7 @@ struct Persist {
       int cs[32];                   // start of each class in the stage
       int capI[32];                 // index of that sample
       WidePivots<KT> wp;            // pivots of segment pivSeg
+      KT q[16];                     // the same 15 pivots as one sorted sequence
       int pivSeg;
     };
     union {

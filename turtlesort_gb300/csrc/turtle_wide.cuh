@@ -95,15 +95,31 @@ __device__ __noinline__ void wide_pivots_warp(const SegDesc* sd, WidePivots<KT>*
   __syncwarp();
 }
 
-// Class (0..30) of key k: the parent's pivots in registers, the children's
-// in shared memory (one load of the child's set per key).
+// The 15 pivots of a two-level pass in key order: child ci's three pivots,
+// then the parent's pivot ci (for ci < 3).  Child ci's pivots lie between the
+// parent pivots around it, so the sequence is sorted.  The class of key k is
+// then 2 * #{q < k} + [k equals the first q not below it]: a key equal to a
+// pivot goes to the first run of that value, every other key to its gap.
+// Lanes 0..14 write the sequence; the caller synchronizes the warp.
 template <typename KT>
-__device__ __forceinline__ unsigned wide_class_of(KT k, const PivotSet<KT>& pp,
-                                                  const PivotSet<KT>* child) {
-  const unsigned c1 = (unsigned)class_lut<KT>(k, pp.p[0], pp.p[1], pp.p[2], pp.lut);
-  const PivotSet<KT> cs = child[(c1 >> 1) & 3u];
-  const unsigned c2 = (unsigned)class_lut<KT>(k, cs.p[0], cs.p[1], cs.p[2], cs.lut);
-  return wide_class(c1, c2);
+__device__ __forceinline__ void wide_sequence(const WidePivots<KT>& wp, KT* q) {
+  const int lane = threadIdx.x & 31;
+  if (lane < 15) {
+    const int ci = lane >> 2, j = lane & 3;
+    q[lane] = j < 3 ? wp.child[ci].p[j] : wp.par.p[ci];
+  }
+}
+
+// Class (0..30) of key k from the sorted 15-pivot sequence (branchless lower
+// bound: four probes, then one equality test).
+template <typename KT>
+__device__ __forceinline__ unsigned wide_class_seq(KT k, const KT* q) {
+  int r = q[7] < k ? 8 : 0;
+  r += q[r + 3] < k ? 4 : 0;
+  r += q[r + 1] < k ? 2 : 0;
+  r += q[r] < k ? 1 : 0;
+  const bool eq = q[r < 15 ? r : 14] == k && r < 15;
+  return 2u * (unsigned)r + (eq ? 1u : 0u);
 }
 
 // Lane counts of one chunk: 4-bit fields, word w = classes 8w..8w+7.
@@ -167,10 +183,11 @@ __device__ __forceinline__ void count31_tile_warp(const SortArgs& a, int pass, i
     chunk_bulk_issue<U, kIdx, false>(ws, 0, src, nullptr, abs0 + (long long)chBeg * kWCH);
   if (td.seg != ws.t.pivSeg) {  // pivots of the warp's last segment are kept
     wide_pivots_warp<KT>(&a.segs[par][td.seg], &ws.t.wp);
+    wide_sequence<KT>(ws.t.wp, ws.t.q);
+    __syncwarp();
     ws.t.pivSeg = td.seg;
   }
-  const PivotSet<KT> pp = ws.t.wp.par;
-  const PivotSet<KT>* child = ws.t.wp.child;
+  const KT* q = ws.t.q;
   unsigned acc8[8];
 #pragma unroll
   for (int w = 0; w < 8; ++w) acc8[w] = 0;
@@ -199,7 +216,7 @@ __device__ __forceinline__ void count31_tile_warp(const SortArgs& a, int pass, i
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
       if (okm >> i & 1u) {
-        const unsigned k = wide_class_of<KT>(key[i], pp, child);
+        const unsigned k = wide_class_seq<KT>(key[i], q);
         wide_bump(acc4, k);
         if (i < 4) cb0 |= k << (8 * i);
         else cb1 |= k << (8 * (i - 4));
