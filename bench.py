@@ -152,6 +152,23 @@ def cpu_baselines(keys: np.ndarray, idx: np.ndarray, threads: int) -> dict:
     }
 
 
+def max_over_ranks(x: float, dist, device) -> float:
+    """The largest x over all ranks (the slowest rank's time), or x itself with
+    one rank.  `device` is where the reduction tensor lives (cuda for NCCL,
+    cpu for gloo)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world: int, n: int, steps: int, slowest_total_s: float) -> float:
+    """Whole-job throughput: the keys of every rank over the slowest rank's time."""
+    return world * n * steps / slowest_total_s
+
+
 def run_reference(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -253,13 +270,11 @@ def run_gpu(args) -> None:
     leaf_ms /= max(nk, 1)
     ms = [a.elapsed_time(b) for a, b in events]
     tot_ms = sum(ms)
+    tot_ms = max_over_ranks(tot_ms, dist, dev)
     if dist is not None:
-        t = torch.tensor([tot_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        tot_ms = float(t.item())
         dist.barrier()
     ms_step = tot_ms / args.steps
-    value = world * n * args.steps / (tot_ms / 1e3)
+    value = job_rate(world, n, args.steps, tot_ms / 1e3)
 
     # full check of the final result against the properties of a sort
     fk = d_k.cpu().numpy()
@@ -284,7 +299,7 @@ def run_gpu(args) -> None:
             e2e_launches += sorter.launches - l0
     if not np.array_equal(hk, fk):
         raise RuntimeError("end-to-end result differs from the device result")
-    e2e_value = world * n * len(e2e_t) / sum(e2e_t)
+    e2e_value = job_rate(world, n, len(e2e_t), max_over_ranks(sum(e2e_t), dist, dev))
 
     if rank != 0:
         return
@@ -342,7 +357,8 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--n", type=int, default=1 << 26)
+    ap.add_argument("--n", "--keys", dest="n", type=int, default=1 << 26,
+                    help="keys per sort (--keys also works under torchrun)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--clocks-csv", default=None)
     ap.add_argument("--workload", default="sort64m",

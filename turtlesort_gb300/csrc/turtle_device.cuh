@@ -545,132 +545,6 @@ __device__ __forceinline__ void block_sort_groups(KT* sk, int* si, int P, int ac
   __syncthreads();
 }
 
-// ---- stable group radix sort (leaves longer than 16 warps' worth of the
-// merge path) ----
-//
-// The CTA's warps are split into groups of Gw warps; group g sorts the n_g
-// elements at smem[g*Gw*32*kItems ...] in place.  Keys are first reduced to
-// (key - min) over the group, so only the bits that differ inside the leaf are
-// sorted (3 eight-bit passes for a typical 32-bit leaf, 1 for bytes).  Each
-// pass is a stable counting scatter: elements are ranked per warp in memory
-// order (warp chunk, round, lane) with __match_any_sync, per-warp digit
-// counters are scanned digit-major inside the group, and every element is
-// written to its new slot.  All threads of the CTA must call it.
-template <typename KT, int kItems, bool kIdx, int NW>
-__device__ __forceinline__ void group_radix_sort(KT* sk, int* si, int n_mine, int Gw,
-                                                 int* cnt /* NW*256 + NW ints */,
-                                                 KT* sred /* 2*NW */, int* spass) {
-  constexpr int kWCH = 32 * kItems;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int g = warp / Gw, wg = warp - g * Gw;  // group, warp inside the group
-  const int gbase = g * Gw * kWCH;              // first element of the group
-  const int wbase = gbase + wg * kWCH;          // first element of this warp
-  unsigned lt;
-  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
-  // 1. min / max over the group
-  KT mn = key_max<KT>(), mx = KT(0);
-  for (int r = 0; r < kItems; ++r) {
-    const int e = wg * kWCH + r * 32 + lane;
-    if (e < n_mine) {
-      const KT k = sk[kpad<KT>(gbase + e)];
-      mn = k < mn ? k : mn;
-      mx = k > mx ? k : mx;
-    }
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const KT a = __shfl_xor_sync(0xffffffffu, mn, o);
-    const KT b = __shfl_xor_sync(0xffffffffu, mx, o);
-    mn = a < mn ? a : mn;
-    mx = b > mx ? b : mx;
-  }
-  if (tid == 0) *spass = 0;
-  if (lane == 0) { sred[warp] = mn; sred[NW + warp] = mx; }
-  __syncthreads();
-  mn = key_max<KT>();
-  mx = KT(0);
-  for (int w = 0; w < Gw; ++w) {
-    const KT a = sred[g * Gw + w], b = sred[NW + g * Gw + w];
-    mn = a < mn ? a : mn;
-    mx = b > mx ? b : mx;
-  }
-  const KT range = (n_mine > 1 && mx > mn) ? KT(mx - mn) : KT(0);
-  int bits = 0;
-  if (range) bits = (sizeof(KT) == 8) ? 64 - __clzll((unsigned long long)range) : 32 - __clz((unsigned)range);
-  const int passes = (bits + 7) >> 3;
-  if (lane == 0 && wg == 0) atomicMax(spass, passes);
-  __syncthreads();
-  const int maxPasses = *spass;
-  int* gcnt = cnt + g * Gw * 256;  // this group's counters, [digit][warp in group]
-  for (int p = 0; p < maxPasses; ++p) {
-    const int shift = p * 8;
-    const bool active = p < passes;
-    // zero the group's counters (each thread: 8 entries)
-    for (int j = (tid - g * Gw * 32); j < Gw * 256; j += Gw * 32) gcnt[j] = 0;
-    KT key[kItems];
-    int id[kItems];
-    unsigned short rk[kItems];
-#pragma unroll
-    for (int r = 0; r < kItems; ++r) {
-      const int e = wg * kWCH + r * 32 + lane;
-      const bool ok = active && e < n_mine;
-      key[r] = ok ? sk[kpad<KT>(gbase + e)] : KT(0);
-      if (kIdx) id[r] = ok ? si[ipad(gbase + e)] : 0;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int r = 0; r < kItems; ++r) {
-      const int e = wg * kWCH + r * 32 + lane;
-      const bool ok = active && e < n_mine;
-      const int d = ok ? (int)(((key[r] - mn) >> shift) & KT(0xff)) : 256 + lane;
-      const unsigned peers = __match_any_sync(0xffffffffu, d);
-      int run = 0;
-      if (ok) run = gcnt[d * Gw + wg];
-      rk[r] = (unsigned short)(run + __popc(peers & lt));
-      __syncwarp();
-      if (ok && (peers >> lane) == 1u) gcnt[d * Gw + wg] = run + __popc(peers);
-      __syncwarp();
-    }
-    __syncthreads();
-    // exclusive scan of the group's 256*Gw counters (digit-major)
-    {
-      const int gt = tid - g * Gw * 32;  // thread index inside the group
-      const int per = 8;                 // 256*Gw / (32*Gw)
-      int v[per];
-      int s = 0;
-#pragma unroll
-      for (int j = 0; j < per; ++j) { v[j] = gcnt[gt * per + j]; s += v[j]; }
-      int inc = s;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += y;
-      }
-      __syncthreads();
-      int* wtot = cnt + NW * 256;        // NW spare ints after the counters
-      if (lane == 31) wtot[warp] = inc;
-      __syncthreads();
-      int pre = 0;
-      for (int w = g * Gw; w < warp; ++w) pre += wtot[w];
-      int run = pre + inc - s;
-#pragma unroll
-      for (int j = 0; j < per; ++j) { gcnt[gt * per + j] = run; run += v[j]; }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int r = 0; r < kItems; ++r) {
-      const int e = wg * kWCH + r * 32 + lane;
-      if (active && e < n_mine) {
-        const int d = (int)(((key[r] - mn) >> shift) & KT(0xff));
-        const int pos = gcnt[d * Gw + wg] + rk[r];
-        sk[kpad<KT>(gbase + pos)] = key[r];
-        if (kIdx) si[ipad(gbase + pos)] = id[r];
-      }
-    }
-    __syncthreads();
-  }
-}
-
 // Size class of a leaf: the smallest power-of-two thread group whose
 // registers hold it (class c uses P = 1 << c threads).
 template <int kItems>

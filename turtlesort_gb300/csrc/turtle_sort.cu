@@ -47,14 +47,9 @@
 
 namespace turtle {
 
-// Leaf size classes: class c uses P = 1 << c threads of the leaf CTA.
-// Classes up to kMergeClassMax use the register network + merge-path groups;
-// larger ones the radix groups of P / 32 warps.
-constexpr int kMergeClassMax = 4;
-// The merge-path groups measured faster than the radix groups for every leaf
-// class on GB300 (with digit peers found by match.any or by one vote per digit
-// bit), so the radix groups are compiled out of the leaf sort.
-constexpr bool kRadixLeaves = false;
+// Leaf size classes: class c uses P = 1 << c threads of the leaf CTA, each
+// group sorted by the register network + merge-path merges (a shared-memory
+// radix sort of the same leaves measured slower for every class on GB300).
 
 constexpr int ilog2(int x) { return x <= 1 ? 0 : 1 + ilog2(x >> 1); }
 #ifndef TURTLE_COUNT_RING
@@ -146,9 +141,6 @@ struct Persist {
   struct LeafSmem {  // leaf / batched CTA
     KT keys[G::kLeafKeySlots];
     int idx[kLIdxSlots];
-    int rcnt[kLWarps * 256 + kLWarps];
-    KT rred[2 * kLWarps];
-    int rpass;
     int item;
     int classOff[16];
     int classItems[16];
@@ -219,29 +211,16 @@ __device__ __forceinline__ long long sample_pos(long long start, long long n, in
   return start + ((2 * (long long)i + 1) * n) / (2 * ns);
 }
 
-// Sorted pivots of a segment: from its captured samples on shallow levels
-// (the sorted three under the reference rule, else the quartiles of the
-// kSamples samples), from samples of its keys on deep ones.
+// Sorted pivots of a segment on deep levels (quartiles of samples of its
+// keys) or under the reference rule (its three captured samples, sorted);
+// segment_pivots_warp ranks the sampled rule's kSamples samples.
 template <typename KT, typename U>
 __device__ __forceinline__ void segment_pivots(const SegDesc* sd, const U* src, int level, KT flip,
                                                int ns, KT* piv) {
   if (level >= kDepthSwitch) {
     sampled_pivots<KT, U>(src, __ldcg(&sd->start), __ldcg(&sd->n), flip, piv);
-  } else if (ns == 3) {
-    sort3<KT>((KT)__ldcg(&sd->samp[0]), (KT)__ldcg(&sd->samp[1]), (KT)__ldcg(&sd->samp[2]), piv);
   } else {
-    // rank of each sample (ties by index): ranks ns/4, ns/2, 3ns/4 are the quartiles
-    for (int i = 0; i < kSamples; ++i) {
-      const KT vi = (KT)__ldcg(&sd->samp[i]);
-      int r = 0;
-      for (int j = 0; j < kSamples; ++j) {
-        const KT vj = (KT)__ldcg(&sd->samp[j]);
-        r += (vj < vi) || (vj == vi && j < i);
-      }
-      if (r == kSamples / 4) piv[0] = vi;
-      if (r == kSamples / 2) piv[1] = vi;
-      if (r == (3 * kSamples) / 4) piv[2] = vi;
-    }
+    sort3<KT>((KT)__ldcg(&sd->samp[0]), (KT)__ldcg(&sd->samp[1]), (KT)__ldcg(&sd->samp[2]), piv);
   }
 }
 
@@ -1367,11 +1346,7 @@ __device__ void sort_leaf_group(const SortArgs& a, int cls, int first, int last,
     if (kIdx) sm.idx[ipad(region + j)] = ok ? srcI[d.start + j] : 0;
   }
   __syncthreads();
-  if (!kRadixLeaves || cls <= kMergeClassMax)
-    block_sort_groups<KT, kItems, kIdx>(sm.keys, sm.idx, P, kLThreads);
-  else
-    group_radix_sort<KT, kItems, kIdx, kLWarps>(sm.keys, sm.idx, d.n, P >> 5, sm.rcnt, sm.rred,
-                                                &sm.rpass);
+  block_sort_groups<KT, kItems, kIdx>(sm.keys, sm.idx, P, kLThreads);
   U* dst = (U*)a.keysA;
   int* dstI = a.idxA;
   for (int j = q; j < d.n; j += P) {
@@ -1480,13 +1455,7 @@ __global__ void __launch_bounds__(kLThreads, 2)
     if (kIdx) sm.idx[ipad(slot)] = idx[base + j];
   }
   __syncthreads();
-  if (!kRadixLeaves || cls <= kMergeClassMax) {
-    block_sort_groups<KT, kItems, kIdx>(sm.keys, sm.idx, P, kLThreads);
-  } else {
-    const int g = tid / P;
-    group_radix_sort<KT, kItems, kIdx, kLWarps>(sm.keys, sm.idx, g < na ? arrSize : 0, P >> 5,
-                                                sm.rcnt, sm.rred, &sm.rpass);
-  }
+  block_sort_groups<KT, kItems, kIdx>(sm.keys, sm.idx, P, kLThreads);
   for (int j = tid; j < total; j += kLThreads) {
     const int g = j / arrSize, e = j - g * arrSize;
     const int slot = g * P * kItems + e;
