@@ -102,9 +102,7 @@ struct SegDesc {        // a segment partitioned by the multi-CTA 3-pivot pass
                                // keys (one-level) or up to kWideSamples keys (two-level)
   int nsamp;            // valid entries of samp (two-level passes)
   unsigned lut;         // class remap for equal pivots, set by the plan
-  unsigned long long pivS[3];  // sorted pivots (unsigned images), set by the plan
-  unsigned long long cpiv[4][3];  // two-level: sorted pivots of the children (classes 0,2,4,6)
-  unsigned clut[4];     // two-level: their class tables
+  unsigned long long pivS[3];  // one-level: sorted pivots (unsigned images), set by the plan
   long long cbase[32];  // class boundaries after planning (one-level: 8, two-level: 32)
   int childSeg[16];     // next-level segments (one-level: 4 children, two-level: 16 grandchildren)
   alignas(16) int tot[32];  // class totals, summed by COUNT (zeroed with 16-byte stores)

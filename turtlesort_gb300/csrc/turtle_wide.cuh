@@ -1,25 +1,24 @@
-// Two-level partition passes of persistent_sort_kernel (sampled pivot rule).
+// Two-level partition passes of persistent_sort_kernel (the default for
+// large sorts; rule TURTLE_PIVOTS_TWO_LEVEL).
 //
-// One pass applies two levels of the 3-pivot partition at once.  Every key is
-// classified by its segment's pivots (class c1 of 7) and, when c1 is not a
-// pivot run, by the pivots of child c1/2 (class c2 of 7).  The 31 classes
-// k = 8*(c1/2) + (c1 odd ? 7 : c2) are in key order, so one stable counting
-// pass (COUNT, PLAN, SCATTER as in the one-level pass) moves every key
-// straight to its grandchild: half the passes over the data, half the grid
-// barriers.  A segment's pivots are the quartiles of its kWideSamples evenly
-// spaced samples; child ci's pivots are the quartiles of the samples that fall
-// in child ci.  SCATTER records the samples of every new grandchild segment
-// as it writes the keys at the sample positions.  Every step is stable, so the
-// output is the stable sort by key whatever the samples are.
+// One pass applies two levels of the 3-pivot partition at once.  A key's
+// class c1 against its segment's pivots (7 classes) and, when c1 is not a
+// pivot run, its class c2 against child c1/2's pivots give one of 31 classes
+// k = 8*(c1/2) + (c1 odd ? 7 : c2), in key order, so one stable counting pass
+// (COUNT, PLAN, SCATTER as in the one-level pass) moves every key straight to
+// its grandchild: half the passes over the data, half the grid barriers.  A
+// segment's pivots are the quartiles of its kWideSamples evenly spaced
+// samples; child ci's pivots are the quartiles of the samples that fall in
+// child ci.  COUNT computes each key's class once (a lower bound over the 15
+// pivots in key order) and stores it as a byte for SCATTER.  SCATTER records
+// the samples of every new grandchild segment as it writes the keys at the
+// sample positions.  Every step is stable, so the output is the stable sort
+// by key whatever the samples are.
 #pragma once
 
 namespace turtle {
 
 constexpr int kWideClasses = 31;  // classes of a two-level pass (class 31 unused)
-
-__device__ __forceinline__ unsigned wide_class(unsigned c1, unsigned c2) {
-  return (c1 >> 1) * 8u + ((c1 & 1u) ? 7u : c2);
-}
 
 // Position of sample i of ns in a segment of m keys starting at pos.
 __device__ __forceinline__ long long wide_sample_pos(long long pos, long long m, int i, int ns) {
@@ -252,8 +251,8 @@ __device__ __forceinline__ void count31_tile_warp(const SortArgs& a, int pass, i
 
 // PLAN of a two-level pass, one plan item (kThreads tiles of one segment):
 // the destination of every tile and class (class bases from the segment's
-// class totals, then the tiles in memory order: stable).  Item 0 also stores
-// the pivots for SCATTER and routes the 31 classes: the parent's pivot runs
+// class totals, then the tiles in memory order: stable).  Item 0 also routes
+// the 31 classes (SCATTER takes the classes from COUNT): the parent's pivot runs
 // and the children's pivot runs are parked for a fill when the keys go to the
 // scratch buffer; a child of at most kLeafMax keys becomes one leaf whatever
 // its second-level classes; every other grandchild becomes a leaf or a
@@ -390,15 +389,7 @@ __device__ __noinline__ void plan31_item(const SortArgs& a, int pass, int item,
       sdp->cbase[31] = sdStart + sm.wcb[32];
     }
     const unsigned pm = __ballot_sync(kFull, park != 0u);
-    if (lane == 0) {
-      sdp->parkMask = pm;
-      for (int q = 0; q < 3; ++q) sdp->pivS[q] = (unsigned long long)sm.wpiv.par.p[q];
-      sdp->lut = sm.wpiv.par.lut;
-      for (int c = 0; c < 4; ++c) {
-        for (int q = 0; q < 3; ++q) sdp->cpiv[c][q] = (unsigned long long)sm.wpiv.child[c].p[q];
-        sdp->clut[c] = sm.wpiv.child[c].lut;
-      }
-    }
+    if (lane == 0) sdp->parkMask = pm;
   }
   __syncthreads();
   if (tid < 16) sdp->childSeg[tid] = sm.gSeg[tid];
@@ -504,15 +495,7 @@ __device__ __noinline__ void plan31_small_warp(const SortArgs& a, int pass, int 
     }
   }
   if (lane < 16) sdp->childSeg[lane] = gseg;
-  if (lane == 0) {
-    sdp->parkMask = pm;
-    for (int q = 0; q < 3; ++q) sdp->pivS[q] = (unsigned long long)wp.par.p[q];
-    sdp->lut = wp.par.lut;
-    for (int c = 0; c < 4; ++c) {
-      for (int q = 0; q < 3; ++q) sdp->cpiv[c][q] = (unsigned long long)wp.child[c].p[q];
-      sdp->clut[c] = wp.child[c].lut;
-    }
-  }
+  if (lane == 0) sdp->parkMask = pm;
   __syncwarp();
 }
 
