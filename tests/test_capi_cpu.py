@@ -88,3 +88,21 @@ def test_server_host_side_checks(native_lib):
     if not has_gpu():
         assert native_lib.turtle_server_create(-1, 1 << 30, 0, 0, C.byref(h)) == 9
         assert not h.value
+
+
+def test_dtype_codes_match_header():
+    """The Python mirror's dtype codes are the C header's enum values."""
+    import re
+    import numpy as np
+    from conftest import ROOT
+    from turtlesort_gb300 import _native, dtype_code
+    text = (ROOT / "include" / "turtle_gb300.h").read_text()
+    enum = dict((m.group(1), int(m.group(2)))
+                for m in re.finditer(r"TURTLE_(\w+) = (\d+)", text.split("turtle_dtype;")[0]))
+    for name, dt in [("INT8", np.int8), ("UINT8", np.uint8), ("INT16", np.int16),
+                     ("UINT16", np.uint16), ("INT32", np.int32), ("UINT32", np.uint32),
+                     ("INT64", np.int64), ("UINT64", np.uint64), ("FLOAT32", np.float32),
+                     ("FLOAT64", np.float64)]:
+        assert enum[name] == getattr(_native, name) == dtype_code(dt), name
+    with pytest.raises(TypeError):
+        dtype_code(np.float16)
