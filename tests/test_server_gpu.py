@@ -141,3 +141,35 @@ def test_server_budget_rejects_what_never_fits():
         st = srv.stats()
     assert np.array_equal(s_copy, np.sort(small))
     assert st["failed"] == 1 and st["completed"] == 1
+
+
+def test_server_float_requests():
+    """float32 / float64 requests (IEEE-754 totalOrder), one of them above the
+    size where batches switch to two-level passes."""
+    _torch_cuda()
+    rng = np.random.default_rng(9)
+
+    def image(x):
+        u = x.view(np.uint32 if x.dtype == np.float32 else np.uint64)
+        sign = u.dtype.type(1) << u.dtype.type(8 * u.itemsize - 1)
+        return np.where((u & sign) != 0, ~u, u | sign)
+
+    reqs = []
+    for r, (dt, n) in enumerate([(np.float32, 1000), (np.float64, 70_000), (np.float32, 9_000_000),
+                                 (np.float64, 5), (np.float32, 300_001)]):
+        x = rng.standard_normal(n).astype(dt)
+        x[:: 97] = np.nan
+        x[1:: 89] = -0.0
+        x[2:: 83] = np.inf
+        idx = np.arange(n, dtype=np.int32) if r % 2 == 0 else None
+        reqs.append((x, x.copy(), None if idx is None else idx.copy(), idx))
+    with ts.TurtleServer(hbm_budget_bytes=8 << 30) as srv:
+        tickets = [srv.submit(k, i) for _, k, i, _ in reqs]
+        for t in tickets:
+            srv.wait(t)
+    for x, k, i, idx in reqs:
+        order = np.argsort(image(x), kind="stable")
+        bits = np.uint32 if x.dtype == np.float32 else np.uint64
+        assert np.array_equal(k.view(bits), x[order].view(bits)), (x.dtype, x.size)
+        if i is not None:
+            assert np.array_equal(i, idx[order]), (x.dtype, x.size)
