@@ -460,10 +460,15 @@ __device__ __forceinline__ int class_lut(KT k, KT p1, KT p2, KT p3, unsigned lut
 // must call it (it synchronizes); only threads below `active` (a multiple of
 // P) touch the arrays, so a CTA whose size is not a multiple of P sorts its
 // complete groups and its remaining threads only take part in the barriers.
+// `nReal` is the number of real keys of the calling thread's group: its tail
+// slots from nReal on hold key_max (id 0) on entry.  After every merge round
+// the first nReal slots of each group hold its real keys and the rest still
+// hold key_max, so a thread whose kItems output slots all lie in the tail
+// skips the register network, the merges and the stores.
 template <typename KT, int kItems, bool kIdx>
-__device__ __forceinline__ void block_sort_groups(KT* sk, int* si, int P, int active) {
+__device__ __forceinline__ void block_sort_groups(KT* sk, int* si, int P, int active, int nReal) {
   const int tid = threadIdx.x;
-  const bool on = tid < active;
+  const bool on = tid < active && (tid & (P - 1)) * kItems < nReal;
   KT k[kItems];
   int v[kItems];
   const int base = tid * kItems;

@@ -1346,7 +1346,7 @@ __device__ void sort_leaf_group(const SortArgs& a, int cls, int first, int last,
     if (kIdx) sm.idx[ipad(region + j)] = ok ? srcI[d.start + j] : 0;
   }
   __syncthreads();
-  block_sort_groups<KT, kItems, kIdx>(sm.keys, sm.idx, P, kLThreads);
+  block_sort_groups<KT, kItems, kIdx>(sm.keys, sm.idx, P, kLThreads, (int)d.n);
   U* dst = (U*)a.keysA;
   int* dstI = a.idxA;
   for (int j = q; j < d.n; j += P) {
@@ -1455,7 +1455,8 @@ __global__ void __launch_bounds__(kLThreads, 2)
     if (kIdx) sm.idx[ipad(slot)] = idx[base + j];
   }
   __syncthreads();
-  block_sort_groups<KT, kItems, kIdx>(sm.keys, sm.idx, P, kLThreads);
+  block_sort_groups<KT, kItems, kIdx>(sm.keys, sm.idx, P, kLThreads,
+                                      tid / P < na ? arrSize : 0);
   for (int j = tid; j < total; j += kLThreads) {
     const int g = j / arrSize, e = j - g * arrSize;
     const int slot = g * P * kItems + e;
