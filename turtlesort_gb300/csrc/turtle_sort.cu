@@ -1340,10 +1340,23 @@ __device__ void sort_leaf_group(const SortArgs& a, int cls, int first, int last,
   if (li < last) d = a.leavesSorted[li];
   const U* src = (const U*)(d.inB ? a.keysB : a.keysA);
   const int* srcI = d.inB ? a.idxB : a.idxA;
-  for (int j = q; j < P * kItems; j += P) {
-    const bool ok = j < d.n;
-    sm.keys[kpad<KT>(region + j)] = ok ? kload<U, KT>(src, d.start + j, flip) : key_max<KT>();
-    if (kIdx) sm.idx[ipad(region + j)] = ok ? srcI[d.start + j] : 0;
+  // a thread's kItems slots are q, q + P, ...: all its loads are issued before
+  // the first shared-memory store, so they overlap instead of queueing
+  {
+    KT lk[kItems];
+    int lv[kItems];
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+      const int j = q + i * P;
+      const bool ok = j < d.n;
+      lk[i] = ok ? kload<U, KT>(src, d.start + j, flip) : key_max<KT>();
+      if (kIdx) lv[i] = ok ? srcI[d.start + j] : 0;
+    }
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+      sm.keys[kpad<KT>(region + q + i * P)] = lk[i];
+      if (kIdx) sm.idx[ipad(region + q + i * P)] = lv[i];
+    }
   }
   __syncthreads();
   block_sort_groups<KT, kItems, kIdx>(sm.keys, sm.idx, P, kLThreads, (int)d.n);
