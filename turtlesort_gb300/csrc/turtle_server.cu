@@ -264,7 +264,6 @@ void worker_loop(turtle_server* s) {
         b->width = head->width;
         b->hasIdx = hasIdx;
         // consecutive waiting requests of the head's group, within limits
-        size_t bytes = 0;
         for (auto it = s->waiting.begin(); it != s->waiting.end();) {
           Request* r = *it;
           if (r->dtype != b->dtype || (r->hostIdx != nullptr) != hasIdx) break;
@@ -282,7 +281,6 @@ void worker_loop(turtle_server* s) {
             }
             break;
           }
-          bytes = need;
           b->reqs.push_back(r);
           b->total += r->n;
           it = s->waiting.erase(it);
@@ -293,7 +291,6 @@ void worker_loop(turtle_server* s) {
           break;  // wait for memory
         }
         b->bytes = batch_bytes(b->width, hasIdx, b->total, (long long)b->reqs.size(), &b->lay);
-        (void)bytes;
         s->inUse += (long long)b->bytes;
         s->inflight++;
         s->batches++;
