@@ -51,7 +51,8 @@ class Bench {
     if (target)
       *target = (size_t)(t2.count() - t1.count());
     else
-      std::cout << (t2.count() - t1.count()) / 1000000000.0 << " seconds" << std::endl;
+      std::cout << static_cast<double>(t2.count() - t1.count()) / 1000000000.0 << " seconds"
+                << std::endl;
   }
 
  private:
