@@ -52,21 +52,18 @@ def peaks() -> tuple[float, str]:
     return 6800.0, "fallback"
 
 
-def profile_traffic(n: int) -> float | None:
-    """DRAM bytes (read + write) per launch of the persistent kernel, from the
-    committed ncu summary of that kernel (the line
-    `traffic_bytes_per_launch_2^26: B`), for the 2^26-element workload only."""
-    p = ROOT / "profiles" / "persistent_sort_kernel_32M_int32_idx.md"
-    if n != 1 << 26 or not p.exists():
-        return None
-    for line in p.read_text().splitlines():
-        line = line.strip()
-        if line.startswith("traffic_bytes_per_launch_2^26:"):
-            try:
-                return float(line.split(":", 1)[1])
-            except ValueError:
-                return None
-    return None
+def profile_traffic(n: int) -> tuple[float | None, str | None]:
+    """DRAM bytes (read + write) per launch of the partition kernel and the
+    ncu summary they come from, for the workload size the figure was scaled
+    to (profiles/traffic.json); (None, None) for other sizes."""
+    p = ROOT / "profiles" / "traffic.json"
+    try:
+        e = json.loads(p.read_text())["persistent_sort_kernel"]
+    except Exception:
+        return None, None
+    if int(e.get("bench_n", -1)) != n:
+        return None, None
+    return float(e["bytes_per_launch"]), e.get("summary")
 
 
 class ClockSampler:
@@ -310,7 +307,7 @@ def run_gpu(args) -> None:
     part_bytes = alg_bytes / 2
     achieved = part_bytes / (part_ms / 1e3) / 1e9
     sort_achieved = alg_bytes / (ms_step / 1e3) / 1e9
-    traffic = profile_traffic(n)
+    traffic, traffic_src = profile_traffic(n)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
@@ -322,6 +319,7 @@ def run_gpu(args) -> None:
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
+                     "traffic_source": traffic_src,
                      "peak_source": f"{peak_kind} hbm_gbs",
                      "kernel": "persistent_sort_kernel<uint32_t,true> (one launch per sort)",
                      "algorithmic_bytes_per_launch": part_bytes,

@@ -251,6 +251,12 @@ const char* turtle_last_cuda_error(const turtle_sorter* s);
  * involved; callers see TURTLE_ERR_OUT_OF_MEMORY. */
 void turtle_debug_fail_allocations(int count);
 
+/* Like turtle_debug_fail_allocations, but only the k-th device-buffer
+ * allocation from now on fails (k = 1: the next one) and the ones before it
+ * succeed, so a test can fail a constructor part-way and check that nothing
+ * it had allocated stays behind.  0 cancels. */
+void turtle_debug_fail_allocation_at(int k);
+
 /* Phase timeline of the last persistent-kernel sort (valid after
  * turtle_stream_status / turtle_sync): globaltimer nanoseconds taken after
  * each grid barrier, with the work items of the phase that ended there, and a
@@ -281,6 +287,14 @@ int turtle_debug_error_site(const turtle_sorter* s, int* site, int* block, int* 
  * more than `leaves` leaves are pending at the start of a level.  0 restores
  * the default (yield only when the lists could overflow). */
 turtle_status turtle_debug_yield_threshold(turtle_sorter* s, int32_t leaves);
+
+/* For testing the bounded device-side waits (no counterpart in the
+ * reference, whose CDP kernels have no waits of their own): later sorts on
+ * this sorter give up a grid-barrier wait after `polls` polls instead of the
+ * default limit (about a second of polling), record TURTLE_ERR_TIMEOUT and
+ * return, leaving the context usable.  0 restores the default.  Only the
+ * grid-barrier wait is shortened; a CTA has no bulk copy in flight there. */
+turtle_status turtle_debug_barrier_polls(turtle_sorter* s, int64_t polls);
 
 /* Library version string (static storage). */
 const char* turtle_version(void);

@@ -240,6 +240,12 @@ class TurtleSort:
         _check(self._lib.turtle_debug_yield_threshold(self._h, int(leaves)), "yield_threshold",
                self._h)
 
+    def barrier_polls(self, polls: int) -> None:
+        """Testing: give up a grid-barrier wait after ``polls`` polls (the
+        sort then reports TURTLE_ERR_TIMEOUT); 0 restores the default."""
+        _check(self._lib.turtle_debug_barrier_polls(self._h, int(polls)), "barrier_polls",
+               self._h)
+
     def kernel_times(self, last: int):
         """(sorts, partition_ms, leaf_ms) summed over the last `last` timed sorts."""
         pm, lm = C.c_double(), C.c_double()

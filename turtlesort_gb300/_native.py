@@ -50,6 +50,7 @@ SIGNATURES = [
     ("turtle_status_string", C.c_char_p, [_I]),
     ("turtle_last_cuda_error", C.c_char_p, [_P]),
     ("turtle_debug_fail_allocations", None, [_I]),
+    ("turtle_debug_fail_allocation_at", None, [_I]),
     ("turtle_version", C.c_char_p, []),
     ("turtle_debug_timeline", _I, [_P, _P, _P, _I]),
     ("turtle_sort_device_noalloc", _I, [_I, _P, _P, _I64, _P]),
@@ -59,6 +60,7 @@ SIGNATURES = [
     ("turtle_debug_kernel_times", _I, [_P, _I, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("turtle_debug_error_site", _I, [_P, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I)]),
     ("turtle_debug_yield_threshold", _I, [_P, C.c_int32]),
+    ("turtle_debug_barrier_polls", _I, [_P, _I64]),
     ("turtle_server_create", _I, [_I, _I64, _I, _I64, C.POINTER(_P)]),
     ("turtle_server_submit", _I, [_P, _I, _P, _P, _I64, C.POINTER(C.c_uint64)]),
     ("turtle_server_poll", _I, [_P, C.c_uint64, C.POINTER(_I)]),

@@ -77,6 +77,7 @@ struct turtle_sorter {
   bool overlapped = false;  // this StartSorting's result copies are queued on copyStream
   bool yielded = false;     // the partition yielded: those copies may be stale
   int leafYield = 0;        // test threshold for yields (0: default)
+  long long barrierPolls = 0;  // test limit of the grid-barrier wait (0: default)
   // optional kernel timing: events around the two launches of each sort
   static constexpr int kRing = 64;
   bool timeKernels = false;
@@ -121,6 +122,7 @@ turtle::SortArgs make_args(turtle_sorter* s, void* keys, int32_t* idx, const lon
                                          s->pivotRule);
   a.slices = slices;
   a.leafYield = s->leafYield;
+  a.barrierPolls = s->barrierPolls;
   return a;
 }
 
@@ -567,6 +569,8 @@ const char* turtle_last_cuda_error(const turtle_sorter* s) {
 
 void turtle_debug_fail_allocations(int count) { turtle::vmm_inject_failures(count); }
 
+void turtle_debug_fail_allocation_at(int k) { turtle::vmm_inject_failure_at(k); }
+
 int turtle_debug_timeline(const turtle_sorter* s, uint64_t* ns, int32_t* info, int max) {
   if (!s || !s->hctrl) return 0;
   const int n = std::min(std::min(s->hctrl->tlCount, turtle::kTimeline), max - 1);
@@ -634,6 +638,14 @@ turtle_status turtle_debug_yield_threshold(turtle_sorter* s, int32_t leaves) {
   std::lock_guard<std::mutex> lk(s->mu);
   s->leafYield = leaves;
   free_graphs(s);  // captured launches carry the old threshold
+  return TURTLE_OK;
+}
+
+turtle_status turtle_debug_barrier_polls(turtle_sorter* s, int64_t polls) {
+  if (!s || polls < 0) return TURTLE_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->barrierPolls = polls;
+  free_graphs(s);  // captured launches carry the old limit
   return TURTLE_OK;
 }
 

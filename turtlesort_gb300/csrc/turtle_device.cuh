@@ -203,6 +203,7 @@ struct SortArgs {
   int leafYield;             // > 0: yield when more leaves are pending (testing)
   int samples;               // pivot samples per segment: 3 (reference rule, one-level
                              // passes) or kWideSamples (sampled rule, two-level passes)
+  long long barrierPolls;    // > 0: grid-barrier poll limit (testing the timeout), else kSpinLimit
   Control* ctrl;
 };
 
@@ -231,10 +232,10 @@ __device__ __forceinline__ void set_error(Control* c, int code, int site = 0, in
 }
 
 // Grid-wide barrier for a cooperatively launched grid.  The spin is bounded:
-// after kSpinLimit polls the CTA records kDevTimeout and leaves; a CTA also
-// leaves as soon as any other CTA has recorded an error.  Returns true when
-// no error is recorded.
-__device__ __forceinline__ bool grid_barrier(Control* c) {
+// after `limit` polls (kSpinLimit unless a test lowers it) the CTA records
+// kDevTimeout and leaves; a CTA also leaves as soon as any other CTA has
+// recorded an error.  Returns true when no error is recorded.
+__device__ __forceinline__ bool grid_barrier(Control* c, long long limit = kSpinLimit) {
   __syncthreads();
   __shared__ int s_err;
   if (threadIdx.x == 0) {
@@ -250,7 +251,7 @@ __device__ __forceinline__ bool grid_barrier(Control* c) {
       unsigned ns = 32;
       while (gen.load(cuda::memory_order_acquire) == g) {
         if (ld_acquire_int(&c->error) != 0) break;
-        if (++it > kSpinLimit) {
+        if (++it > limit) {
           set_error(c, kDevTimeout, kSiteBarrier, (int)g);
           break;
         }

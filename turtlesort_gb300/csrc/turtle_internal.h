@@ -47,5 +47,8 @@ bool vmm_compression_supported(int device);
 // Test hook: make the next `count` VMM allocations fail (host-side fault
 // injection; the buffer layer then reports cudaErrorMemoryAllocation).
 void vmm_inject_failures(int count);
+// Test hook: only the k-th device-buffer allocation from now on fails (k = 1:
+// the next one); 0 cancels.
+void vmm_inject_failure_at(int k);
 
 }  // namespace turtle

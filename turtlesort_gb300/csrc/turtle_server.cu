@@ -188,23 +188,42 @@ turtle_status finish_batch(turtle_server* s, Batch* b) {
   // a partition that yielded (leaf lists full) continues here before the
   // results are trusted; pathological inputs only
   int rounds = 0;
-  while (sl.hCtrl->error == 0 && sl.hCtrl->yield != 0 && rounds++ < 100000) {
-    b->args.resume = 1;
-    turtle::kernels_launch_persistent(b->width, b->hasIdx, b->args,
-                                      s->grid[b->width][b->hasIdx ? 1 : 0], s->sSort);
-    cudaMemcpyAsync(sl.hCtrl, b->args.ctrl, sizeof(turtle::Control), cudaMemcpyDeviceToHost,
-                    s->sSort);
-    cudaStreamSynchronize(s->sSort);
-    for (Request* r : b->reqs) {
-      if (r->n <= 0) continue;
-      const char* keys = b->dev;
-      cudaMemcpyAsync(r->hostKeys, keys + r->offset * b->width, (size_t)r->n * b->width,
-                      cudaMemcpyDeviceToHost, s->sSort);
-      if (b->hasIdx)
-        cudaMemcpyAsync(r->hostIdx, (const int*)b->args.idxA + r->offset, (size_t)r->n * 4,
-                        cudaMemcpyDeviceToHost, s->sSort);
+  while (sl.hCtrl->error == 0 && sl.hCtrl->yield != 0) {
+    if (++rounds > 100000) {
+      st = TURTLE_ERR_CAPACITY;  // still yielding: the keys are only partly sorted
+      break;
     }
-    cudaStreamSynchronize(s->sSort);
+    b->args.resume = 1;
+    cudaError_t e = turtle::kernels_launch_persistent(b->width, b->hasIdx, b->args,
+                                                      s->grid[b->width][b->hasIdx ? 1 : 0],
+                                                      s->sSort);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(sl.hCtrl, b->args.ctrl, sizeof(turtle::Control),
+                          cudaMemcpyDeviceToHost, s->sSort);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->sSort);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      st = TURTLE_ERR_CUDA;
+      break;
+    }
+  }
+  // the copy-out that ran before the relaunches read partly sorted keys:
+  // copy the finished result again
+  if (rounds > 0 && st == TURTLE_OK && sl.hCtrl->error == 0) {
+    cudaError_t e = cudaSuccess;
+    for (Request* r : b->reqs) {
+      if (r->n <= 0 || e != cudaSuccess) continue;
+      e = cudaMemcpyAsync(r->hostKeys, b->dev + r->offset * b->width, (size_t)r->n * b->width,
+                          cudaMemcpyDeviceToHost, s->sSort);
+      if (e == cudaSuccess && b->hasIdx)
+        e = cudaMemcpyAsync(r->hostIdx, (const int*)b->args.idxA + r->offset, (size_t)r->n * 4,
+                            cudaMemcpyDeviceToHost, s->sSort);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->sSort);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      st = TURTLE_ERR_CUDA;
+    }
   }
   if (sl.hCtrl->error == turtle::kDevTimeout) st = TURTLE_ERR_TIMEOUT;
   else if (sl.hCtrl->error == turtle::kDevCapacity) st = TURTLE_ERR_CAPACITY;

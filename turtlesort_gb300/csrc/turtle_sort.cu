@@ -1069,6 +1069,7 @@ __device__ __noinline__ bool leaf_bucket(const SortArgs& a, typename Persist<U, 
   constexpr int kItems = Geom<U>::kLItems;
   constexpr int kB = kMaxSlices * 16;
   Control* c = a.ctrl;
+  const long long polls = a.barrierPolls > 0 ? a.barrierPolls : kSpinLimit;
   const int tid = threadIdx.x;
   const int S = a.slices;
   const int nLeaves = ld_acquire_int(&c->leafCount);
@@ -1085,7 +1086,7 @@ __device__ __noinline__ bool leaf_bucket(const SortArgs& a, typename Persist<U, 
   __syncthreads();
   for (int b = tid; b < S * 16; b += kThreads)
     if (sm.classItems[b]) atomicAdd(&c->classCount[b], sm.classItems[b]);
-  if (!grid_barrier(c)) return false;
+  if (!grid_barrier(c, polls)) return false;
   timeline_mark(c, nl);
   // bucket 2: scatter into per-bucket ranges
   if (tid == 0) {
@@ -1118,7 +1119,7 @@ __device__ __noinline__ bool leaf_bucket(const SortArgs& a, typename Persist<U, 
     }
     c->fillItems = nf;
   }
-  if (!grid_barrier(c)) return false;
+  if (!grid_barrier(c, polls)) return false;
   timeline_mark(c, nf);
   return true;
 }
@@ -1170,6 +1171,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
   extern __shared__ __align__(16) unsigned char smem_raw[];
   typename P::Smem& sm = *reinterpret_cast<typename P::Smem*>(smem_raw);
   Control* c = a.ctrl;
+  const long long polls = a.barrierPolls > 0 ? a.barrierPolls : kSpinLimit;
   const int tid = threadIdx.x;
   typename P::WarpArea& ws = sm.w[tid >> 5];
   unsigned mphase = 0;  // parity bit of each chunk buffer's barrier
@@ -1218,7 +1220,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
       route_input<U, kTile, kLeafMax>(a, s, e - s, true, &si, &tb, &nt);
     }
   }
-  if (!grid_barrier(c)) return;
+  if (!grid_barrier(c, polls)) return;
   timeline_mark(c, 0);
 
   // one level adds at most 4 leaves and 3 fills (+ chunks) per segment, a
@@ -1251,7 +1253,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
     stream_tiles<U, kIdx, 0, kWide>(a, level, ntiles, &c->work[phase & 3], ws, mphase);
     ++phase;
     __threadfence();
-    if (!grid_barrier(c)) return;
+    if (!grid_barrier(c, polls)) return;
     timeline_mark(c, ntiles);
 
     // PLAN, first step when a segment has several plan items: item totals
@@ -1265,7 +1267,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
       }
       ++phase;
       __threadfence();
-      if (!grid_barrier(c)) return;
+      if (!grid_barrier(c, polls)) return;
     }
     // PLAN: one item (kThreads tiles of one segment) per CTA
     {
@@ -1292,7 +1294,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
       ++phase;
     }
     __threadfence();
-    if (!grid_barrier(c)) return;
+    if (!grid_barrier(c, polls)) return;
     timeline_mark(c, nsegs);
 
     // SCATTER
@@ -1309,7 +1311,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
     stream_tiles<U, kIdx, 1, kWide>(a, level, ntiles, &c->work[phase & 3], ws, mphase);
     ++phase;
     __threadfence();
-    if (!grid_barrier(c)) return;
+    if (!grid_barrier(c, polls)) return;
     timeline_mark(c, nsegs);
   }
   if (blockIdx.x == 0 && tid == 0) c->levels = wide ? 2 * level : level;

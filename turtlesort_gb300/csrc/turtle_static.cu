@@ -19,10 +19,13 @@
 //   * the first call on a device resolves the array's device address with
 //     cudaGetSymbolAddress (and prepares the kernels); make that first call
 //     before any stream capture;
-//   * the call waits for its stream and returns the device-side status;
+//   * the call waits for its own stream (the status words are read with one
+//     copy ordered on that stream) and returns the device-side status;
 //   * nothing here calls cudaMalloc, cudaFree or any other allocating routine.
 #include <cuda_runtime.h>
 
+#include <cstddef>
+#include <cstring>
 #include <mutex>
 
 #include "../../include/turtle_gb300.h"
@@ -120,16 +123,23 @@ extern "C" turtle_status turtle_sort_device_noalloc(turtle_dtype dtype, void* d_
   for (int round = 0;; ++round) {
     e = turtle::kernels_launch_persistent(width, hasIdx, a, st->grid[width][hasIdx ? 1 : 0], cs);
     if (e != cudaSuccess) return cuda_status(e);
+    // the status words (Control::error .. Control::yield) in one copy ordered
+    // on the caller's stream, so the call waits for its own work only
+    constexpr size_t kFrom = offsetof(turtle::Control, error);
+    constexpr size_t kTo = offsetof(turtle::Control, yield) + sizeof(int);
+    static_assert(kFrom < kTo, "error precedes yield in the control block");
+    unsigned char words[kTo - kFrom];
+    if ((e = cudaMemcpyAsync(words, (const unsigned char*)a.ctrl + kFrom, kTo - kFrom,
+                             cudaMemcpyDeviceToHost, cs)) != cudaSuccess)
+      return cuda_status(e);
     if ((e = cudaStreamSynchronize(cs)) != cudaSuccess) return cuda_status(e);
-    int word[2] = {0, 0};  // Control::error, Control::yield
-    if ((e = cudaMemcpy(&word[0], &a.ctrl->error, sizeof(int), cudaMemcpyDeviceToHost)) != cudaSuccess)
-      return cuda_status(e);
-    if ((e = cudaMemcpy(&word[1], &a.ctrl->yield, sizeof(int), cudaMemcpyDeviceToHost)) != cudaSuccess)
-      return cuda_status(e);
-    if (word[0] == turtle::kDevTimeout) return TURTLE_ERR_TIMEOUT;
-    if (word[0] == turtle::kDevCapacity) return TURTLE_ERR_CAPACITY;
-    if (word[0] != 0) return TURTLE_ERR_CUDA;
-    if (!word[1]) return TURTLE_OK;
+    int error = 0, yielded = 0;
+    std::memcpy(&error, words, sizeof(int));
+    std::memcpy(&yielded, words + (kTo - kFrom - sizeof(int)), sizeof(int));
+    if (error == turtle::kDevTimeout) return TURTLE_ERR_TIMEOUT;
+    if (error == turtle::kDevCapacity) return TURTLE_ERR_CAPACITY;
+    if (error != 0) return TURTLE_ERR_CUDA;
+    if (!yielded) return TURTLE_OK;
     if (round > 100000) return TURTLE_ERR_CAPACITY;
     a.resume = 1;  // the leaf lists filled up: continue from the saved level
   }

@@ -45,6 +45,7 @@ struct DriverApi {
 std::once_flag g_once;
 DriverApi g_api;
 std::atomic<int> g_inject{0};
+std::atomic<int> g_injectAt{0};  // > 0: the allocation this many calls ahead fails
 
 template <typename F>
 bool resolve(const char* name, F* fn) {
@@ -149,6 +150,8 @@ bool vmm_compression_supported(int device) {
 
 void vmm_inject_failures(int count) { g_inject.store(count < 0 ? 0 : count); }
 
+void vmm_inject_failure_at(int k) { g_injectAt.store(k < 0 ? 0 : k); }
+
 cudaError_t vmm_alloc(DevBuffer* b, size_t bytes, int device, bool want_compression) {
   *b = DevBuffer();
   if (bytes == 0) bytes = 256;
@@ -156,6 +159,8 @@ cudaError_t vmm_alloc(DevBuffer* b, size_t bytes, int device, bool want_compress
     g_inject.fetch_sub(1);
     return cudaErrorMemoryAllocation;
   }
+  if (g_injectAt.load() > 0 && g_injectAt.fetch_sub(1) == 1)
+    return cudaErrorMemoryAllocation;  // the one chosen allocation fails
   if (want_compression && vmm_compression_supported(device) && vmm_try(b, bytes, device, true))
     return cudaSuccess;
   if (vmm_try(b, bytes, device, false)) return cudaSuccess;

@@ -19,6 +19,9 @@ Workloads (seeds are ``0x7475727431 + k`` for workload k):
 """
 from __future__ import annotations
 
+import os
+from concurrent.futures import ThreadPoolExecutor
+
 import numpy as np
 
 GAMMA = np.uint64(0x9E3779B97F4A7C15)
@@ -58,6 +61,20 @@ def dtype_range(dtype) -> tuple[int, int]:
     return int(info.min), int(info.max)
 
 
+def _chunked(n: int, fill) -> None:
+    """Calls fill(c0, c) for the CHUNK-sized pieces of [0, n), on several
+    threads for large n (numpy's array loops release the GIL).  The values do
+    not depend on the split: every element is a function of its index."""
+    starts = list(range(0, n, CHUNK))
+    workers = min(len(starts), os.cpu_count() or 1, 16)
+    if workers <= 1:
+        for c0 in starts:
+            fill(c0, min(CHUNK, n - c0))
+        return
+    with ThreadPoolExecutor(workers) as ex:
+        list(ex.map(lambda c0: fill(c0, min(CHUNK, n - c0)), starts))
+
+
 def uniform(dtype, n: int, seed: int, lo: int | None = None, hi: int | None = None,
             start: int = 0) -> np.ndarray:
     """n keys uniform in [lo, hi] (default: the dtype's full range)."""
@@ -65,9 +82,11 @@ def uniform(dtype, n: int, seed: int, lo: int | None = None, hi: int | None = No
     lo = dlo if lo is None else lo
     hi = dhi if hi is None else hi
     out = np.empty(n, dtype=dtype)
-    for c0 in range(0, n, CHUNK):
-        c = min(CHUNK, n - c0)
+
+    def fill(c0, c):
         out[c0:c0 + c] = _map_range(splitmix64(seed, start + c0, c), lo, hi, dtype)
+
+    _chunked(n, fill)
     return out
 
 
@@ -131,8 +150,10 @@ def zipf_cdf(s: float = 1.1, ranks: int = 65536) -> np.ndarray:
 def zipf_u16(n: int, seed: int, s: float = 1.1) -> np.ndarray:
     cdf = zipf_cdf(s)
     out = np.empty(n, dtype=np.uint16)
-    for c0 in range(0, n, CHUNK):
-        c = min(CHUNK, n - c0)
+
+    def fill(c0, c):
         u = uniform_real(c, seed, c0)
         out[c0:c0 + c] = np.minimum(np.searchsorted(cdf, u, side="right"), 65535)
+
+    _chunked(n, fill)
     return out
