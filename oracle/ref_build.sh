@@ -13,9 +13,10 @@
 # -lcuda -lcudadevrt).  One change is needed for GCC: the MultiSort member
 # template re-declares the class's template parameter `Type`
 # (turtle-sort.cuh:265,266,272), which MSVC accepts and GCC rejects; the
-# staged copy renames it to MType on those three lines only.  `char` is
-# signed on x86 and unsigned on Arm; -fsigned-char keeps the reference's
-# `char` instantiation a signed 8-bit key on both.
+# staged copy renames it to MType on those three lines only.  The reference's
+# 8-bit signed key type is `char` (turtle-sort.cu:999-1019), which is signed
+# on x86 and unsigned on Arm; nvcc's device code follows the host ABI, so on
+# an Arm host the reference sorts `char` keys in unsigned order.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 OUT="$HERE/_ref"
@@ -36,7 +37,7 @@ case "${1:-build}" in
     test -f "$SRC/turtle-sort.cu" || { echo "no staged reference sources in $SRC" >&2; exit 1; }
     NVCC="${NVCC:-$(command -v nvcc || echo /usr/local/cuda/bin/nvcc)}"
     "$NVCC" -std=c++17 -O3 -rdc=true -gencode arch=compute_103a,code=sm_103a \
-        -Xcompiler -fsigned-char -w -I "$SRC" \
+        -w -I "$SRC" \
         "$HERE/ref_driver.cu" "$SRC/turtle-sort.cu" \
         -o "$OUT/turtle_ref" -lcuda -lcudadevrt
     echo "built $OUT/turtle_ref"

@@ -23,6 +23,7 @@
 // same layout.
 #include "turtle-sort.cuh"
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -58,7 +59,10 @@ int run_sort(const std::string& name, long long n, bool ids, int reps, const std
     std::printf("%s: cannot read input\n", name.c_str());
     return 1;
   }
-  Turtle::TurtleSort<T> sorter((int)n);
+  // capacity of at least 64: StartSorting copies two task pairs (4 ints)
+  // into task buffers of maxN ints even for a single task
+  // (turtle-sort.cuh:172), which fails for maxN < 4
+  Turtle::TurtleSort<T> sorter((int)std::max<long long>(n, 64));
   std::vector<T> firstK;
   std::vector<int> firstI;
   for (int r = 0; r < reps; ++r) {
@@ -106,7 +110,8 @@ int run_case(const std::string& line) {
   int ids = 0, reps = 1;
   if (!(is >> name >> type >> n >> ids >> reps >> in >> out)) return 0;  // blank / comment
   const bool withIds = ids != 0;
-  if (type == "i8") return run_sort<char>(name, n, withIds, reps, in, out);  // built -fsigned-char
+  // int8 keys: the reference's `char` instantiation (unsigned on Arm hosts)
+  if (type == "i8") return run_sort<char>(name, n, withIds, reps, in, out);
   if (type == "u8") return run_sort<unsigned char>(name, n, withIds, reps, in, out);
   if (type == "i16") return run_sort<short>(name, n, withIds, reps, in, out);
   if (type == "u16") return run_sort<unsigned short>(name, n, withIds, reps, in, out);

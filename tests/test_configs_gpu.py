@@ -16,10 +16,16 @@ CPU, run on all host cores) on the same seeded input:
 
 Keys must be bit-identical; ids must be the oracle's stable permutation (the
 GB300 partition and leaf sorts are stable, so ties keep their input order).
+Where the reference's own sort ran the same input (tests/golden/
+ref_outputs.json: distributions a-e, int64, uint8 and the Zipf keys, keys
+only), the keys must also equal the reference's output bytes.
 """
 from __future__ import annotations
 
+import hashlib
+import json
 import os
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -30,6 +36,20 @@ from turtlesort_gb300 import datagen as dg
 pytestmark = pytest.mark.gpu
 
 THREADS = os.cpu_count() or 1
+REF = json.loads((Path(__file__).resolve().parent / "golden" / "ref_outputs.json")
+                 .read_text())["cases"]
+
+
+def _sha(a) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def _expect_reference(case, keys_in, keys_out):
+    """The reference's own sort of the same input gave these bytes."""
+    e = REF[case]
+    assert e["ran"] and e["keys_sorted"]
+    assert _sha(keys_in) == e["input_sha256"], f"{case}: input differs from the reference run's"
+    assert _sha(keys_out) == e["keys_sha256"], f"{case}: keys differ from the reference's output"
 
 
 def _pinned_copy(torch, arr):
@@ -76,6 +96,7 @@ def test_distribution_2p26(gpu, oracle_mod, kind):
         s.Sync()
         _expect_equal("keys (StartSorting, pinned)", hk, ek)
         _expect_equal("ids (StartSorting, pinned)", hi, ei)
+        _expect_reference(f"sweep_{kind}_2p26", keys, hk)
         # the device-resident form on the same input
         dk = torch.from_numpy(keys).cuda()
         di = torch.from_numpy(idx).cuda()
@@ -128,6 +149,7 @@ def test_int64_2p28_with_index(gpu, oracle_mod):
         s.Sync()
     _expect_equal("keys", k, ek)
     _expect_equal("ids", i, ei)
+    _expect_reference("int64_2p28", keys, k)
 
 
 def test_uint8_2p30_keys_only(gpu, oracle_mod):
@@ -138,6 +160,7 @@ def test_uint8_2p30_keys_only(gpu, oracle_mod):
         s.StartSorting(k)
         s.Sync()
     _expect_equal("keys", k, ek)
+    _expect_reference("uint8_2p30", keys, k)
 
 
 def test_uint16_zipf_2p29_keys_only(gpu, oracle_mod):
@@ -148,3 +171,4 @@ def test_uint16_zipf_2p29_keys_only(gpu, oracle_mod):
         s.StartSorting(k)
         s.Sync()
     _expect_equal("keys", k, ek)
+    _expect_reference("uint16_zipf_2p29", keys, k)

@@ -8,9 +8,10 @@
 //    reference's (start, stop) int task arrays (turtle-sort.cuh:41-46) and its
 //    CDP task flip (turtle-sort.cu:35-111).
 //  * a bounded grid barrier for the persistent cooperative kernel.
-//  * the stable one-CTA shared-memory sort (register odd-even transposition +
-//    merge-path merges) that replaces sortByNetwork (turtle-sort.cu:392-559)
-//    and bruteSort (turtle-sort.cu:118-188).
+//  * the stable one-CTA shared-memory sort (packed key/position words, a
+//    register sorting network + merge-path merges) that replaces
+//    sortByNetwork (turtle-sort.cu:392-559) and bruteSort
+//    (turtle-sort.cu:118-188).
 #pragma once
 
 #include <cuda/atomic>
@@ -74,17 +75,7 @@ struct Geom {
   static constexpr int kTile = kPartTile;               // partition tile
   static constexpr int kLeafMax = kLThreads * kLItems;  // shared-memory sort capacity
   static constexpr int kWarpChunk = 32 * kItems;        // elements per warp chunk
-  static constexpr int kKeyPadShift = sizeof(KT) == 8 ? 4 : 5;
-  static constexpr int kLeafKeySlots = kLeafMax + (kLeafMax >> kKeyPadShift) + 8;
-  static constexpr int kLeafIdxSlots = kLeafMax + (kLeafMax >> 5) + 8;
 };
-
-// Bank-conflict padding for shared-memory element arrays.
-template <typename KT>
-__device__ __forceinline__ int kpad(int p) {
-  return p + (p >> (sizeof(KT) == 8 ? 4 : 5));
-}
-__device__ __forceinline__ int ipad(int p) { return p + (p >> 5); }
 
 template <typename KT>
 __device__ __forceinline__ KT key_max() {
@@ -449,102 +440,217 @@ __device__ __forceinline__ int class_lut(KT k, KT p1, KT p2, KT p3, unsigned lut
   return (int)((lut >> (3 * cp)) & 7u);
 }
 
-// ---- stable one-CTA shared-memory sort ----
+// ---- stable one-CTA shared-memory sort of packed words ----
 //
+// The shared-memory sort (leaves, MultiSort arrays) moves one word per key.
+// With ids, the key is packed with its position in its array, so every word
+// is distinct: any sorting network or merge then yields the stable order
+// (ties by position), and each id is fetched once, by position, when the
+// result is written out.  Without ids the word is the key itself (equal keys
+// are indistinguishable, so stability does not arise).  Padding slots hold
+// the largest word, which sorts behind every real one.
+template <typename U, bool kIdx> struct LeafWord;
+
+// 8- and 16-bit keys: (key << 16 | position), 32-bit words.
+template <bool kIdx>
+struct LeafWordNarrow {
+  using W = uint32_t;
+  __device__ __forceinline__ static W make(uint32_t k, int pos) {
+    return kIdx ? (k << 16) | (uint32_t)pos : k;
+  }
+  __device__ __forceinline__ static uint32_t key(W w) { return kIdx ? w >> 16 : w; }
+  __device__ __forceinline__ static int pos(W w) { return (int)(w & 0xFFFFu); }
+  __device__ __forceinline__ static bool less(W a, W b) { return a < b; }
+  __device__ __forceinline__ static W sent() { return ~0u; }
+};
+template <bool kIdx> struct LeafWord<uint8_t, kIdx> : LeafWordNarrow<kIdx> {};
+template <bool kIdx> struct LeafWord<uint16_t, kIdx> : LeafWordNarrow<kIdx> {};
+
+// 32-bit keys: the key alone, or (key << 32 | position).
+template <>
+struct LeafWord<uint32_t, false> {
+  using W = uint32_t;
+  __device__ __forceinline__ static W make(uint32_t k, int) { return k; }
+  __device__ __forceinline__ static uint32_t key(W w) { return w; }
+  __device__ __forceinline__ static int pos(W) { return 0; }
+  __device__ __forceinline__ static bool less(W a, W b) { return a < b; }
+  __device__ __forceinline__ static W sent() { return ~0u; }
+};
+template <>
+struct LeafWord<uint32_t, true> {
+  using W = unsigned long long;
+  __device__ __forceinline__ static W make(uint32_t k, int pos) {
+    return ((W)k << 32) | (uint32_t)pos;
+  }
+  __device__ __forceinline__ static uint32_t key(W w) { return (uint32_t)(w >> 32); }
+  __device__ __forceinline__ static int pos(W w) { return (int)(uint32_t)w; }
+  __device__ __forceinline__ static bool less(W a, W b) { return a < b; }
+  __device__ __forceinline__ static W sent() { return ~0ull; }
+};
+
+// 64-bit keys: the key alone, or the key with its position beside it.
+template <>
+struct LeafWord<uint64_t, false> {
+  using W = unsigned long long;
+  __device__ __forceinline__ static W make(unsigned long long k, int) { return k; }
+  __device__ __forceinline__ static unsigned long long key(W w) { return w; }
+  __device__ __forceinline__ static int pos(W) { return 0; }
+  __device__ __forceinline__ static bool less(W a, W b) { return a < b; }
+  __device__ __forceinline__ static W sent() { return ~0ull; }
+};
+struct alignas(16) KeyPos64 {
+  unsigned long long k;
+  unsigned p;
+};
+template <>
+struct LeafWord<uint64_t, true> {
+  using W = KeyPos64;
+  __device__ __forceinline__ static W make(unsigned long long k, int pos) {
+    W w;
+    w.k = k;
+    w.p = (unsigned)pos;
+    return w;
+  }
+  __device__ __forceinline__ static unsigned long long key(W w) { return w.k; }
+  __device__ __forceinline__ static int pos(W w) { return (int)w.p; }
+  __device__ __forceinline__ static bool less(W a, W b) {
+    return a.k < b.k || (a.k == b.k && a.p < b.p);
+  }
+  __device__ __forceinline__ static W sent() {
+    W w;
+    w.k = ~0ull;
+    w.p = ~0u;
+    return w;
+  }
+};
+
+// Bank-conflict padding for word arrays: one spare slot per 128 bytes, so a
+// thread's kItems consecutive words (blocked layout) start in another bank
+// than its neighbour's.
+template <typename W>
+__device__ __forceinline__ int wpad(int p) {
+  return p + p / (int)(128 / sizeof(W));
+}
+template <typename W>
+constexpr int word_slots(int n) {
+  return n + n / (int)(128 / sizeof(W)) + 8;
+}
+
+template <class LW>
+__device__ __forceinline__ void cex(typename LW::W& a, typename LW::W& b) {
+  const bool sw = LW::less(b, a);
+  const typename LW::W lo = sw ? b : a;
+  const typename LW::W hi = sw ? a : b;
+  a = lo;
+  b = hi;
+}
+
+// Batcher's odd-even merge sort of N register words (63 comparators for 16,
+// 19 for 8; each list passes the 0-1 principle on all 2^N inputs).  The
+// comparators are written out so every index is a literal and the words stay
+// in registers.
+template <class LW, int N> struct Network;
+template <class LW>
+struct Network<LW, 8> {
+  __device__ __forceinline__ static void sort(typename LW::W* v) {
+#define TURTLE_C(x, y) cex<LW>(v[x], v[y]);
+    TURTLE_C(0,1) TURTLE_C(2,3) TURTLE_C(4,5) TURTLE_C(6,7) TURTLE_C(0,2) TURTLE_C(1,3)
+    TURTLE_C(4,6) TURTLE_C(5,7) TURTLE_C(1,2) TURTLE_C(5,6) TURTLE_C(0,4) TURTLE_C(1,5)
+    TURTLE_C(2,6) TURTLE_C(3,7) TURTLE_C(2,4) TURTLE_C(3,5) TURTLE_C(1,2) TURTLE_C(3,4)
+    TURTLE_C(5,6)
+  }
+};
+template <class LW>
+struct Network<LW, 16> {
+  __device__ __forceinline__ static void sort(typename LW::W* v) {
+    TURTLE_C(0,1) TURTLE_C(2,3) TURTLE_C(4,5) TURTLE_C(6,7) TURTLE_C(8,9) TURTLE_C(10,11)
+    TURTLE_C(12,13) TURTLE_C(14,15) TURTLE_C(0,2) TURTLE_C(1,3) TURTLE_C(4,6) TURTLE_C(5,7)
+    TURTLE_C(8,10) TURTLE_C(9,11) TURTLE_C(12,14) TURTLE_C(13,15) TURTLE_C(1,2) TURTLE_C(5,6)
+    TURTLE_C(9,10) TURTLE_C(13,14) TURTLE_C(0,4) TURTLE_C(1,5) TURTLE_C(2,6) TURTLE_C(3,7)
+    TURTLE_C(8,12) TURTLE_C(9,13) TURTLE_C(10,14) TURTLE_C(11,15) TURTLE_C(2,4) TURTLE_C(3,5)
+    TURTLE_C(10,12) TURTLE_C(11,13) TURTLE_C(1,2) TURTLE_C(3,4) TURTLE_C(5,6) TURTLE_C(9,10)
+    TURTLE_C(11,12) TURTLE_C(13,14) TURTLE_C(0,8) TURTLE_C(1,9) TURTLE_C(2,10) TURTLE_C(3,11)
+    TURTLE_C(4,12) TURTLE_C(5,13) TURTLE_C(6,14) TURTLE_C(7,15) TURTLE_C(4,8) TURTLE_C(5,9)
+    TURTLE_C(6,10) TURTLE_C(7,11) TURTLE_C(2,4) TURTLE_C(3,5) TURTLE_C(6,8) TURTLE_C(7,9)
+    TURTLE_C(10,12) TURTLE_C(11,13) TURTLE_C(1,2) TURTLE_C(3,4) TURTLE_C(5,6) TURTLE_C(7,8)
+    TURTLE_C(9,10) TURTLE_C(11,12) TURTLE_C(13,14)
+#undef TURTLE_C
+  }
+};
+
 // The CTA is split into groups of P threads (P a power of two); group g sorts
-// the kItems*P elements in smem[g*P*kItems, (g+1)*P*kItems) of the key and id
-// arrays (unused tail slots hold key_max and come last, so real keys equal to
-// key_max stay in front of them).  Each thread sorts kItems consecutive
-// elements in registers by odd-even transposition (stable), then log2(P)
-// rounds of merge-path merges (ties taken from the left run) produce the
-// sorted group.  Results are left in shared memory.  All threads of the CTA
-// must call it (it synchronizes); only threads below `active` (a multiple of
-// P) touch the arrays, so a CTA whose size is not a multiple of P sorts its
-// complete groups and its remaining threads only take part in the barriers.
-// `nReal` is the number of real keys of the calling thread's group: its tail
-// slots from nReal on hold key_max (id 0) on entry.  After every merge round
-// the first nReal slots of each group hold its real keys and the rest still
-// hold key_max, so a thread whose kItems output slots all lie in the tail
-// skips the register network, the merges and the stores.
-template <typename KT, int kItems, bool kIdx>
-__device__ __forceinline__ void block_sort_groups(KT* sk, int* si, int P, int active, int nReal) {
+// the kItems*P words in sw[g*P*kItems, (g+1)*P*kItems) (addressed through
+// wpad).  Each thread sorts its kItems consecutive words in registers, then
+// log2(P) rounds of merge-path merges double the sorted runs; a round whose
+// two runs lie inside one warp synchronizes that warp only.  Results are left
+// in sw.  All threads of the CTA must call it; only threads below `active`
+// (a multiple of P) touch the words.  `nReal` is the number of real words of
+// the calling thread's group, in front of its padding: a thread whose kItems
+// output slots all lie at or after nReal holds only padding after every
+// round (padding sorts last), so it skips the network, the merges and the
+// stores.
+template <class LW, int kItems>
+__device__ __forceinline__ void block_sort_words(typename LW::W* sw, int P, int active,
+                                                 int nReal) {
+  using W = typename LW::W;
   const int tid = threadIdx.x;
-  const bool on = tid < active && (tid & (P - 1)) * kItems < nReal;
-  KT k[kItems];
-  int v[kItems];
-  const int base = tid * kItems;
-#pragma unroll
-  for (int i = 0; i < kItems; ++i) {
-    k[i] = on ? sk[kpad<KT>(base + i)] : KT(0);
-    if (kIdx) v[i] = on ? si[ipad(base + i)] : 0;
-  }
-  // odd-even transposition: swap only on strict inversion -> stable
-#pragma unroll
-  for (int r = 0; r < kItems; ++r) {
-#pragma unroll
-    for (int i = (r & 1); i + 1 < kItems; i += 2) {
-      if (k[i + 1] < k[i]) {
-        KT t = k[i]; k[i] = k[i + 1]; k[i + 1] = t;
-        if (kIdx) { int u = v[i]; v[i] = v[i + 1]; v[i + 1] = u; }
-      }
-    }
-  }
   const int lane_in_group = tid & (P - 1);
-  const int group_first = tid - lane_in_group;
-  for (int w = 1; w < P; w <<= 1) {
-    // registers -> smem (blocked)
-    __syncthreads();
-    if (on) {
-#pragma unroll
-      for (int i = 0; i < kItems; ++i) {
-        sk[kpad<KT>(base + i)] = k[i];
-        if (kIdx) si[ipad(base + i)] = v[i];
-      }
-    }
-    __syncthreads();
-    if (!on) continue;
-    // merge runs of w threads pairwise: my pair starts at thread pf
-    const int pair_lane = lane_in_group & (2 * w - 1);
-    const int pf = tid - pair_lane;
-    const int a0 = pf * kItems;
-    const int len = w * kItems;
-    const int b0 = a0 + len;
-    const int diag = pair_lane * kItems;
-    int lo = diag > len ? diag - len : 0;
-    int hi = diag < len ? diag : len;
-    while (lo < hi) {
-      const int mid = (lo + hi) >> 1;
-      // take more from A while A[mid] <= B[diag-1-mid]
-      if (!(sk[kpad<KT>(b0 + diag - 1 - mid)] < sk[kpad<KT>(a0 + mid)])) lo = mid + 1;
-      else hi = mid;
-    }
-    int ia = lo, ib = diag - lo;
-    KT ka = ia < len ? sk[kpad<KT>(a0 + ia)] : key_max<KT>();
-    KT kb = ib < len ? sk[kpad<KT>(b0 + ib)] : key_max<KT>();
-#pragma unroll
-    for (int i = 0; i < kItems; ++i) {
-      const bool takeA = (ib >= len) || (ia < len && !(kb < ka));
-      if (takeA) {
-        k[i] = ka;
-        if (kIdx) v[i] = si[ipad(a0 + ia)];
-        ++ia;
-        ka = ia < len ? sk[kpad<KT>(a0 + ia)] : key_max<KT>();
-      } else {
-        k[i] = kb;
-        if (kIdx) v[i] = si[ipad(b0 + ib)];
-        ++ib;
-        kb = ib < len ? sk[kpad<KT>(b0 + ib)] : key_max<KT>();
-      }
-    }
-  }
-  (void)group_first;
-  __syncthreads();
+  const bool on = tid < active && lane_in_group * kItems < nReal;
+  const int base = tid * kItems;
+  W v[kItems];
   if (on) {
 #pragma unroll
-    for (int i = 0; i < kItems; ++i) {
-      sk[kpad<KT>(base + i)] = k[i];
-      if (kIdx) si[ipad(base + i)] = v[i];
+    for (int i = 0; i < kItems; ++i) v[i] = sw[wpad<W>(base + i)];
+    Network<LW, kItems>::sort(v);
+  }
+  for (int w = 1; w < P; w <<= 1) {
+    const bool inWarp = 2 * w <= 32;  // the pair of runs lies in one warp
+    if (inWarp) __syncwarp(); else __syncthreads();
+    if (on) {
+#pragma unroll
+      for (int i = 0; i < kItems; ++i) sw[wpad<W>(base + i)] = v[i];
     }
+    if (inWarp) __syncwarp(); else __syncthreads();
+    if (on) {
+      // merge runs A = [a0, a0+len) and B = [b0, b0+len) of the pair; this
+      // thread produces merged outputs [diag, diag + kItems)
+      const int pair_lane = lane_in_group & (2 * w - 1);
+      const int a0 = (tid - pair_lane) * kItems;
+      const int len = w * kItems;
+      const int b0 = a0 + len;
+      const int diag = pair_lane * kItems;
+      int lo = diag > len ? diag - len : 0;
+      int hi = diag < len ? diag : len;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        // take more from A while A[mid] <= B[diag-1-mid] (ties from A: stable)
+        if (!LW::less(sw[wpad<W>(b0 + diag - 1 - mid)], sw[wpad<W>(a0 + mid)])) lo = mid + 1;
+        else hi = mid;
+      }
+      int ia = lo, ib = diag - lo;
+      W a = ia < len ? sw[wpad<W>(a0 + ia)] : LW::sent();
+      W b = ib < len ? sw[wpad<W>(b0 + ib)] : LW::sent();
+#pragma unroll
+      for (int i = 0; i < kItems; ++i) {
+        const bool takeB = LW::less(b, a);
+        v[i] = takeB ? b : a;
+        ia += takeB ? 0 : 1;
+        ib += takeB ? 1 : 0;
+        if (i + 1 < kItems) {
+          // one load: the next word of the run the output came from
+          const int r = takeB ? ib : ia;
+          const int at = takeB ? b0 + ib : a0 + ia;
+          const W x = r < len ? sw[wpad<W>(at)] : LW::sent();
+          a = takeB ? a : x;
+          b = takeB ? x : b;
+        }
+      }
+    }
+  }
+  if (P <= 32) __syncwarp(); else __syncthreads();
+  if (on) {
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) sw[wpad<W>(base + i)] = v[i];
   }
   __syncthreads();
 }

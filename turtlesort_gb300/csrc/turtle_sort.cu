@@ -137,10 +137,11 @@ struct Persist {
     WidePivots<KT> wpiv;
   };
 
-  static constexpr int kLIdxSlots = kIdx ? G::kLeafIdxSlots : 4;
+  using LW = LeafWord<U, kIdx>;
+  using LWord = typename LW::W;
   struct LeafSmem {  // leaf / batched CTA
-    KT keys[G::kLeafKeySlots];
-    int idx[kLIdxSlots];
+    LWord words[word_slots<LWord>(G::kLeafMax)];  // packed key (+ position) words
+    int idx[kIdx ? G::kLeafMax + 8 : 4];           // ids by position
     int item;
     int classOff[16];
     int classItems[16];
@@ -1344,6 +1345,8 @@ __device__ void sort_leaf_group(const SortArgs& a, int cls, int first, int last,
   const int* srcI = d.inB ? a.idxB : a.idxA;
   // a thread's kItems slots are q, q + P, ...: all its loads are issued before
   // the first shared-memory store, so they overlap instead of queueing
+  using LW = typename P_::LW;
+  using W = typename LW::W;
   {
     KT lk[kItems];
     int lv[kItems];
@@ -1351,22 +1354,25 @@ __device__ void sort_leaf_group(const SortArgs& a, int cls, int first, int last,
     for (int i = 0; i < kItems; ++i) {
       const int j = q + i * P;
       const bool ok = j < d.n;
-      lk[i] = ok ? kload<U, KT>(src, d.start + j, flip) : key_max<KT>();
+      lk[i] = ok ? kload<U, KT>(src, d.start + j, flip) : KT(0);
       if (kIdx) lv[i] = ok ? srcI[d.start + j] : 0;
     }
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
-      sm.keys[kpad<KT>(region + q + i * P)] = lk[i];
-      if (kIdx) sm.idx[ipad(region + q + i * P)] = lv[i];
+      const int j = q + i * P;
+      const bool ok = j < d.n;
+      sm.words[wpad<W>(region + j)] = ok ? LW::make(lk[i], j) : LW::sent();
+      if (kIdx && ok) sm.idx[region + j] = lv[i];
     }
   }
   __syncthreads();
-  block_sort_groups<KT, kItems, kIdx>(sm.keys, sm.idx, P, kLThreads, (int)d.n);
+  block_sort_words<LW, kItems>(sm.words, P, kLThreads, (int)d.n);
   U* dst = (U*)a.keysA;
   int* dstI = a.idxA;
   for (int j = q; j < d.n; j += P) {
-    kstore<U, KT>(dst, d.start + j, sm.keys[kpad<KT>(region + j)], flip);
-    if (kIdx) dstI[d.start + j] = sm.idx[ipad(region + j)];
+    const W w = sm.words[wpad<W>(region + j)];
+    kstore<U, KT>(dst, d.start + j, (KT)LW::key(w), flip);
+    if (kIdx) dstI[d.start + j] = sm.idx[region + LW::pos(w)];
   }
   __syncthreads();
 }
@@ -1454,29 +1460,28 @@ __global__ void __launch_bounds__(kLThreads, 2)
   const long long na = (numArrays - first) < groups ? (numArrays - first) : groups;
   const long long base = first * arrSize;
   const int total = (int)(na * arrSize);
+  using LW = typename P_::LW;
+  using W = typename LW::W;
   // pad every group's tail
   {
     const int g = tid / P, q = tid & (P - 1);
-    for (int j = arrSize + q; j < P * kItems; j += P) {
-      sm.keys[kpad<KT>(g * P * kItems + j)] = key_max<KT>();
-      if (kIdx) sm.idx[ipad(g * P * kItems + j)] = 0;
-    }
+    for (int j = arrSize + q; j < P * kItems; j += P) sm.words[wpad<W>(g * P * kItems + j)] = LW::sent();
   }
   // coalesced load of the whole range
   for (int j = tid; j < total; j += kLThreads) {
     const int g = j / arrSize, e = j - g * arrSize;
     const int slot = g * P * kItems + e;
-    sm.keys[kpad<KT>(slot)] = kload<U, KT>(keys, base + j, flip);
-    if (kIdx) sm.idx[ipad(slot)] = idx[base + j];
+    sm.words[wpad<W>(slot)] = LW::make(kload<U, KT>(keys, base + j, flip), e);
+    if (kIdx) sm.idx[slot] = idx[base + j];
   }
   __syncthreads();
-  block_sort_groups<KT, kItems, kIdx>(sm.keys, sm.idx, P, kLThreads,
-                                      tid / P < na ? arrSize : 0);
+  block_sort_words<LW, kItems>(sm.words, P, kLThreads, tid / P < na ? arrSize : 0);
   for (int j = tid; j < total; j += kLThreads) {
     const int g = j / arrSize, e = j - g * arrSize;
-    const int slot = g * P * kItems + e;
-    kstore<U, KT>(keys, base + j, sm.keys[kpad<KT>(slot)], flip);
-    if (kIdx) idx[base + j] = sm.idx[ipad(slot)];
+    const int region = g * P * kItems;
+    const W w = sm.words[wpad<W>(region + e)];
+    kstore<U, KT>(keys, base + j, (KT)LW::key(w), flip);
+    if (kIdx) idx[base + j] = sm.idx[region + LW::pos(w)];
   }
 }
 
