@@ -139,12 +139,21 @@ struct Persist {
 
   using LW = LeafWord<U, kIdx>;
   using LWord = typename LW::W;
+  // word arrays of the shared-memory sort: full-range words, or (leaves)
+  // range-packed 32-bit words or, for 64-bit keys with ids, 64-bit words
+  static constexpr size_t kLeafWordBytes =
+      sizeof(LWord) * (size_t)word_slots<LWord>(G::kLeafMax) > 8 * (size_t)word_slots<uint64_t>(G::kLeafMax)
+          ? sizeof(LWord) * (size_t)word_slots<LWord>(G::kLeafMax)
+          : 8 * (size_t)word_slots<uint64_t>(G::kLeafMax);
   struct LeafSmem {  // leaf / batched CTA
-    LWord words[word_slots<LWord>(G::kLeafMax)];  // packed key (+ position) words
-    int idx[kIdx ? G::kLeafMax + 8 : 4];           // ids by position
+    alignas(16) unsigned char wbytes[kLeafWordBytes];  // packed key (+ position) words
+    int idx[kIdx ? G::kLeafMax + 8 : 4];                // ids by position
+    KT gmin[kLWarps], gmax[kLWarps];                    // per-warp key range of the loaded leaves
+    KT glo[kLThreads];                                  // smallest key of each group's leaf
     int item;
     int classOff[16];
     int classItems[16];
+    __device__ LWord* words() { return reinterpret_cast<LWord*>(wbytes); }
   };
 };
 
@@ -1324,8 +1333,60 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
 // LEAF kernel
 // ---------------------------------------------------------------------------
 
+// Sort the loaded leaves of the CTA's groups as words of codec LW and write
+// keys and ids to A.  Each thread's raw keys wait in the word buffer at the
+// slots it wrote; the group's smallest key is `lo`.  What the output needs
+// after the sort (the leaf descriptor, lo) is reloaded then, which keeps the
+// sort within the register budget.
+template <typename U, bool kIdx, class LW>
+__device__ __forceinline__ void leaf_words_sort(const SortArgs& a,
+                                                typename Persist<U, kIdx>::LeafSmem& sm, int P,
+                                                int li, int last,
+                                                typename Persist<U, kIdx>::KT lo) {
+  using KT = typename Persist<U, kIdx>::KT;
+  using W = typename LW::W;
+  constexpr int kItems = Geom<U>::kLItems;
+  const int tid = threadIdx.x;
+  const int g = tid / P, q = tid & (P - 1);
+  const int n = li < last ? __ldcg(&a.leavesSorted[li].n) : 0;
+  W* words = reinterpret_cast<W*>(sm.wbytes);
+  {
+    const int region = g * P * kItems;
+    KT lk[kItems];
+    const KT* raw = reinterpret_cast<const KT*>(sm.wbytes);
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) lk[i] = raw[region + q + i * P];
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+      const int j = q + i * P;
+      words[wpad<W>(region + j)] = j < n ? LW::make(lk[i], lo, j) : LW::sent();
+    }
+  }
+  if (q == 0) sm.glo[g] = lo;
+  __syncthreads();
+  block_sort_words<LW, kItems>(words, P, kLThreads, n);
+  if (li < last) {
+    const LeafDesc d = a.leavesSorted[li];
+    const KT base = sm.glo[g];
+    const int region = g * P * kItems;
+    U* dst = (U*)a.keysA;
+    int* dstI = a.idxA;
+    const KT flip = (KT)a.flip;
+    for (int j = q; j < d.n; j += P) {
+      const W w = words[wpad<W>(region + j)];
+      kstore<U, KT>(dst, d.start + j, (KT)LW::key(w, base), flip);
+      if (kIdx) dstI[d.start + j] = sm.idx[region + LW::pos(w)];
+    }
+  }
+}
+
 // Sort up to kLThreads/P leaves of size class cls (P = 1 << cls threads each)
-// from leavesSorted[first, last), results to A.
+// from leavesSorted[first, last), results to A.  The keys are loaded once;
+// when every leaf of the CTA spans a narrow key range (the leaves of the
+// partition lie between two pivots) they are sorted as range-packed 32-bit
+// words (64-bit words for 64-bit keys with ids when that range fits), else as
+// full-range words.
 template <typename U, bool kIdx>
 __device__ void sort_leaf_group(const SortArgs& a, int cls, int first, int last,
                                 typename Persist<U, kIdx>::LeafSmem& sm) {
@@ -1333,7 +1394,7 @@ __device__ void sort_leaf_group(const SortArgs& a, int cls, int first, int last,
   using KT = typename P_::KT;
   constexpr int kItems = Geom<U>::kLItems;
   const int P = 1 << cls;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int g = tid / P, q = tid & (P - 1);
   const int li = first + g;
   const int region = g * P * kItems;
@@ -1344,9 +1405,10 @@ __device__ void sort_leaf_group(const SortArgs& a, int cls, int first, int last,
   const U* src = (const U*)(d.inB ? a.keysB : a.keysA);
   const int* srcI = d.inB ? a.idxB : a.idxA;
   // a thread's kItems slots are q, q + P, ...: all its loads are issued before
-  // the first shared-memory store, so they overlap instead of queueing
-  using LW = typename P_::LW;
-  using W = typename LW::W;
+  // the first shared-memory store, so they overlap instead of queueing.  Keys
+  // and ids go to shared memory as loaded (ids are fetched by position once
+  // the words are sorted); the thread keeps the range of its keys.
+  KT tmin = key_max<KT>(), tmax = KT(0);
   {
     KT lk[kItems];
     int lv[kItems];
@@ -1357,22 +1419,46 @@ __device__ void sort_leaf_group(const SortArgs& a, int cls, int first, int last,
       lk[i] = ok ? kload<U, KT>(src, d.start + j, flip) : KT(0);
       if (kIdx) lv[i] = ok ? srcI[d.start + j] : 0;
     }
+    KT* raw = reinterpret_cast<KT*>(sm.wbytes);
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
       const int j = q + i * P;
-      const bool ok = j < d.n;
-      sm.words[wpad<W>(region + j)] = ok ? LW::make(lk[i], j) : LW::sent();
-      if (kIdx && ok) sm.idx[region + j] = lv[i];
+      if (j < d.n) {
+        tmin = lk[i] < tmin ? lk[i] : tmin;
+        tmax = lk[i] > tmax ? lk[i] : tmax;
+        if (kIdx) sm.idx[region + j] = lv[i];
+      }
+      raw[region + j] = lk[i];
     }
   }
-  __syncthreads();
-  block_sort_words<LW, kItems>(sm.words, P, kLThreads, (int)d.n);
-  U* dst = (U*)a.keysA;
-  int* dstI = a.idxA;
-  for (int j = q; j < d.n; j += P) {
-    const W w = sm.words[wpad<W>(region + j)];
-    kstore<U, KT>(dst, d.start + j, (KT)LW::key(w), flip);
-    if (kIdx) dstI[d.start + j] = sm.idx[region + LW::pos(w)];
+  // key range of the group: its lanes, then its warps
+  const int span = P < 32 ? P : 32;
+  for (int o = 1; o < span; o <<= 1) {
+    const KT m0 = __shfl_xor_sync(kFull, tmin, o), m1 = __shfl_xor_sync(kFull, tmax, o);
+    tmin = m0 < tmin ? m0 : tmin;
+    tmax = m1 > tmax ? m1 : tmax;
+  }
+  if (P > 32) {
+    if (lane == 0) { sm.gmin[warp] = tmin; sm.gmax[warp] = tmax; }
+    __syncthreads();
+    const int w0 = (g * P) >> 5;
+    for (int w = w0; w < w0 + (P >> 5); ++w) {
+      tmin = sm.gmin[w] < tmin ? sm.gmin[w] : tmin;
+      tmax = sm.gmax[w] > tmax ? sm.gmax[w] : tmax;
+    }
+  }
+  const unsigned long long range = d.n > 0 ? (unsigned long long)(tmax - tmin) : 0ull;
+  using Narrow = RangeWord<KT, uint32_t, kIdx>;
+  using Mid = RangeWord<KT, uint64_t, kIdx>;
+  using Full = FullWord<U, kIdx>;
+  // 8/16-bit keys and 32-bit keys without ids already sort 32-bit words
+  constexpr bool kNarrowOpt = !(sizeof(U) <= 2 || (sizeof(U) == 4 && !kIdx));
+  if (kNarrowOpt && __syncthreads_and(range <= Narrow::kMaxRange)) {
+    leaf_words_sort<U, kIdx, Narrow>(a, sm, P, li, last, tmin);
+  } else if (sizeof(U) == 8 && kIdx && __syncthreads_and(range <= Mid::kMaxRange)) {
+    leaf_words_sort<U, kIdx, Mid>(a, sm, P, li, last, tmin);
+  } else {
+    leaf_words_sort<U, kIdx, Full>(a, sm, P, li, last, tmin);
   }
   __syncthreads();
 }
@@ -1465,21 +1551,21 @@ __global__ void __launch_bounds__(kLThreads, 2)
   // pad every group's tail
   {
     const int g = tid / P, q = tid & (P - 1);
-    for (int j = arrSize + q; j < P * kItems; j += P) sm.words[wpad<W>(g * P * kItems + j)] = LW::sent();
+    for (int j = arrSize + q; j < P * kItems; j += P) sm.words()[wpad<W>(g * P * kItems + j)] = LW::sent();
   }
   // coalesced load of the whole range
   for (int j = tid; j < total; j += kLThreads) {
     const int g = j / arrSize, e = j - g * arrSize;
     const int slot = g * P * kItems + e;
-    sm.words[wpad<W>(slot)] = LW::make(kload<U, KT>(keys, base + j, flip), e);
+    sm.words()[wpad<W>(slot)] = LW::make(kload<U, KT>(keys, base + j, flip), e);
     if (kIdx) sm.idx[slot] = idx[base + j];
   }
   __syncthreads();
-  block_sort_words<LW, kItems>(sm.words, P, kLThreads, tid / P < na ? arrSize : 0);
+  block_sort_words<LW, kItems>(sm.words(), P, kLThreads, tid / P < na ? arrSize : 0);
   for (int j = tid; j < total; j += kLThreads) {
     const int g = j / arrSize, e = j - g * arrSize;
     const int region = g * P * kItems;
-    const W w = sm.words[wpad<W>(region + e)];
+    const W w = sm.words()[wpad<W>(region + e)];
     kstore<U, KT>(keys, base + j, (KT)LW::key(w), flip);
     if (kIdx) idx[base + j] = sm.idx[region + LW::pos(w)];
   }

@@ -121,43 +121,6 @@ __device__ __forceinline__ unsigned wide_class_seq(KT k, const KT* q) {
   return 2u * (unsigned)r + (eq ? 1u : 0u);
 }
 
-// Lane counts of one chunk: 4-bit fields, word w = classes 8w..8w+7.
-__device__ __forceinline__ void wide_bump(unsigned* acc4, unsigned k) {
-  const unsigned w = k >> 3, inc = 1u << (4u * (k & 7u));
-  acc4[0] += w == 0u ? inc : 0u;
-  acc4[1] += w == 1u ? inc : 0u;
-  acc4[2] += w == 2u ? inc : 0u;
-  acc4[3] += w == 3u ? inc : 0u;
-}
-
-// Widen a word of eight 4-bit fields to two words of four 8-bit fields.
-__device__ __forceinline__ unsigned widen_lo(unsigned x) {
-  return (x & 0xFu) | ((x & 0xF0u) << 4) | ((x & 0xF00u) << 8) | ((x & 0xF000u) << 12);
-}
-__device__ __forceinline__ unsigned widen_hi(unsigned x) {
-  return ((x >> 16) & 0xFu) | ((x >> 12) & 0xF00u) | ((x >> 8) & 0xF0000u) |
-         ((x >> 4) & 0xF000000u);
-}
-
-// Warp totals of eight words of four 8-bit fields (classes 4w..4w+3): lane k
-// returns the total of class k.  One reduction per two classes (16-bit sums).
-__device__ __forceinline__ int wide_totals(const unsigned* a8) {
-  const int lane = threadIdx.x & 31;
-  int mine = 0;
-#pragma unroll
-  for (int w = 0; w < 8; ++w) {
-    const unsigned x = a8[w];
-    const unsigned lo = __reduce_add_sync(0xffffffffu, (x & 0xFFu) | ((x & 0xFF00u) << 8));
-    const unsigned hi = __reduce_add_sync(0xffffffffu, ((x >> 16) & 0xFFu) | ((x >> 8) & 0xFF0000u));
-    const int k0 = 4 * w;
-    if (lane == k0) mine = (int)(lo & 0xFFFFu);
-    if (lane == k0 + 1) mine = (int)(lo >> 16);
-    if (lane == k0 + 2) mine = (int)(hi & 0xFFFFu);
-    if (lane == k0 + 3) mine = (int)(hi >> 16);
-  }
-  return mine;
-}
-
 // COUNT of a two-level pass: tile t's 31 class counts go to its row of
 // tileCnt and each key's class to its byte of a.cls (for SCATTER); the warp's
 // running class totals of the segment (accSeg / accCnt, lane k holds class k)
@@ -187,9 +150,17 @@ __device__ __forceinline__ void count31_tile_warp(const SortArgs& a, int pass, i
     ws.t.pivSeg = td.seg;
   }
   const KT* q = ws.t.q;
-  unsigned acc8[8];
+  // per-lane class tallies, one byte each (a lane sees at most kTile / 32 =
+  // 64 keys of a tile): cnt[32 * k + lane], in the stage buffer, which COUNT
+  // does not use otherwise
+  static_assert(sizeof(ws.sk) >= 32 * 32, "the stage holds 32 x 32 byte tallies");
+  unsigned char* cnt = reinterpret_cast<unsigned char*>(ws.sk);
+  {
+    unsigned* z = reinterpret_cast<unsigned*>(cnt);
 #pragma unroll
-  for (int w = 0; w < 8; ++w) acc8[w] = 0;
+    for (int j = 0; j < 8; ++j) z[32 * j + lane] = 0u;
+  }
+  __syncwarp();
   for (int ch = chBeg; ch < chEnd; ++ch) {
     const int b = (ch - chBeg) & 1;
     const long long c0 = abs0 + (long long)ch * kWCH;
@@ -210,13 +181,12 @@ __device__ __forceinline__ void count31_tile_warp(const SortArgs& a, int pass, i
     } else {
       load_chunk<U, KT, kItems>(src + abs0, abs0, a.n, e0, rlo, rhi, flip, key);
     }
-    unsigned acc4[4] = {0u, 0u, 0u, 0u};
     unsigned cb0 = 0, cb1 = 0;  // the keys' classes, one byte each, for SCATTER
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
       if (okm >> i & 1u) {
         const unsigned k = wide_class_seq<KT>(key[i], q);
-        wide_bump(acc4, k);
+        cnt[32 * k + lane] += 1;
         if (i < 4) cb0 |= k << (8 * i);
         else cb1 |= k << (8 * (i - 4));
       }
@@ -232,14 +202,17 @@ __device__ __forceinline__ void count31_tile_warp(const SortArgs& a, int pass, i
           if (okm >> i & 1u) cdst[i] = (unsigned char)((i < 4 ? cb0 >> (8 * i) : cb1 >> (8 * (i - 4))) & 0xFFu);
       }
     }
-#pragma unroll
-    for (int w = 0; w < 4; ++w) {
-      acc8[2 * w] += widen_lo(acc4[w]);
-      acc8[2 * w + 1] += widen_hi(acc4[w]);
-    }
     __syncwarp();
   }
-  const int mine = wide_totals(acc8);
+  // lane k sums class k's 32 lane tallies (four bytes per word)
+  unsigned sum = 0u;
+  {
+    const unsigned* row = reinterpret_cast<const unsigned*>(cnt + 32 * lane);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) sum = __dp4a(row[j], 0x01010101u, sum);
+  }
+  const int mine = (int)sum;
+  __syncwarp();
   a.tileCnt[par][(long long)t * kRow + lane] = mine;
   if (td.seg != accSeg) {
     if (accSeg >= 0 && accCnt) atomicAdd(&a.segs[par][accSeg].tot[lane], accCnt);
