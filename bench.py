@@ -273,6 +273,15 @@ def run_gpu(args) -> None:
     ms_step = tot_ms / args.steps
     value = job_rate(world, n, args.steps, tot_ms / 1e3)
 
+    # the same steps under the compile-time default configuration (the table
+    # disabled), for the tuned-against-default comparison
+    sorter.set_tuning(False)
+    ev_default = [one_step(True) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    sorter.status(sh)
+    sorter.set_tuning(True)
+    default_ms = sum(a.elapsed_time(b) for a, b in ev_default) / args.steps
+
     # full check of the final result against the properties of a sort
     fk = d_k.cpu().numpy()
     fi = d_i.cpu().numpy()
@@ -336,6 +345,11 @@ def run_gpu(args) -> None:
                 "gpu_launches_per_step": e2e_launches / len(e2e_t),
                 "overlap": "leaf phase in position slices; each finished slice is copied to the "
                            "host while later slices sort"},
+        "tuning": {"table": ts.tuning_source(),
+                   "config": ts.tuning_lookup(np.int32, True, n),
+                   "tuned_ms_per_step": ms_step,
+                   "default_config_ms_per_step": default_ms,
+                   "speedup": default_ms / ms_step},
         "gpu_launches": int(launches),
         "wall_s_timed": t_wall,
         "levels": sorter.last_levels,

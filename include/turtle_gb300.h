@@ -296,6 +296,55 @@ turtle_status turtle_debug_yield_threshold(turtle_sorter* s, int32_t leaves);
  * grid-barrier wait is shortened; a CTA has no bulk copy in flight there. */
 turtle_status turtle_debug_barrier_polls(turtle_sorter* s, int64_t polls);
 
+/* ---- launch configuration (autotuning) ----
+ *
+ * The reference fixes its kernel geometry at compile time
+ * (turtle-sort.cu:7,12; MultiSort's ArrSize / BlockSize template parameters,
+ * turtle-multi-sort.cuh:11,13).  Here each sort picks, by key type, index
+ * flag and size band, a configuration from a table that the project's tuner
+ * (turtlesort_gb300/tune.py) measured on the GPU and compiled into the
+ * library: pass form (TURTLE_PIVOTS_SAMPLED one-level or
+ * TURTLE_PIVOTS_TWO_LEVEL), partition tile (1 << tile_shift keys, shift
+ * 10..12), shared-memory sort geometry (0..3, see turtle_leaf_geometry), leaf
+ * cut (segments of at most leaf_cut keys are sorted in shared memory; 1024 up
+ * to the geometry's capacity) and partition grid (resident CTAs / grid_div,
+ * grid_div 1, 2 or 4).  The output never depends on the configuration. */
+
+/* enable != 0 (default): sorts use the tuned table; 0: the compile-time
+ * defaults (the configuration before tuning). */
+turtle_status turtle_set_tuning(turtle_sorter* s, int enable);
+
+/* Pins one configuration for every later sort on this sorter (form < 0
+ * returns to the table).  May reallocate the sorter's work lists, after
+ * waiting for the device.  TURTLE_ERR_INVALID_ARGUMENT for values outside the
+ * ranges above. */
+turtle_status turtle_set_config(turtle_sorter* s, int form, int tile_shift, int leaf_geometry,
+                                int leaf_cut, int grid_div);
+
+/* The table's configuration for n keys: out5 = {form, tile_shift,
+ * leaf_geometry, leaf_cut, grid_div}. */
+turtle_status turtle_tuning_lookup(turtle_dtype dtype, int track_index, int64_t n, int32_t* out5);
+
+/* The table's shared-memory geometry for MultiSort arrays of arr_size keys
+ * (-1: none listed; the default geometry is used). */
+int turtle_tuning_multisort_geometry(turtle_dtype dtype, int track_index, int64_t arr_size);
+
+/* Where the table came from (device, date), static storage. */
+const char* turtle_tuning_source(void);
+
+/* Shared-memory sort geometry g (0..3) for this key type: out4 = {CTA
+ * threads, keys per thread, capacity, size classes}.  Returns 0 for bad
+ * arguments. */
+int turtle_leaf_geometry(turtle_dtype dtype, int geometry, int32_t* out4);
+
+/* For the tuner and tests: MultiSort of num_arrays arrays of arr_size keys in
+ * device memory with shared-memory geometry `geometry` (no sorter needed;
+ * asynchronous on `stream`, NULL = the legacy default stream).
+ * TURTLE_ERR_TOO_LARGE when the arrays exceed the geometry's capacity. */
+turtle_status turtle_debug_multisort_geometry(turtle_dtype dtype, void* d_keys, int32_t* d_idx,
+                                              int64_t arr_size, int64_t num_arrays, int geometry,
+                                              void* stream);
+
 /* Library version string (static storage). */
 const char* turtle_version(void);
 

@@ -23,7 +23,7 @@ from . import _native
 from ._native import TurtleError
 
 __all__ = ["TurtleSort", "TurtleServer", "TurtleError", "dtype_code", "smem_capacity",
-           "load_library"]
+           "load_library", "tuning_lookup", "leaf_geometry", "tuning_source"]
 
 _DTYPES = {
     np.dtype(np.int8): _native.INT8,
@@ -240,6 +240,25 @@ class TurtleSort:
         _check(self._lib.turtle_debug_yield_threshold(self._h, int(leaves)), "yield_threshold",
                self._h)
 
+    # -- launch configuration (the output never depends on it) --
+    def set_tuning(self, enable: bool = True) -> None:
+        """Use the tuned configuration table (default) or the compile-time
+        defaults."""
+        _check(self._lib.turtle_set_tuning(self._h, int(enable)), "set_tuning", self._h)
+
+    def set_config(self, form: str, tile_shift: int, geometry: int, leaf_cut: int,
+                   grid_div: int = 1) -> None:
+        """Pin a launch configuration: form 'sampled' (one-level passes) or
+        'two_level', tile of 1 << tile_shift keys, shared-memory geometry
+        0..3, leaf cut, partition grid divisor 1/2/4."""
+        code = {"sampled": 1, "two_level": 2}[form]
+        _check(self._lib.turtle_set_config(self._h, code, int(tile_shift), int(geometry),
+                                           int(leaf_cut), int(grid_div)), "set_config", self._h)
+
+    def clear_config(self) -> None:
+        """Back to the tuned table after set_config."""
+        _check(self._lib.turtle_set_config(self._h, -1, 0, 0, 0, 0), "clear_config", self._h)
+
     def barrier_polls(self, polls: int) -> None:
         """Testing: give up a grid-barrier wait after ``polls`` polls (the
         sort then reports TURTLE_ERR_TIMEOUT); 0 restores the default."""
@@ -251,6 +270,28 @@ class TurtleSort:
         pm, lm = C.c_double(), C.c_double()
         n = self._lib.turtle_debug_kernel_times(self._h, int(last), C.byref(pm), C.byref(lm))
         return int(n), float(pm.value), float(lm.value)
+
+
+def tuning_lookup(dtype, track_index: bool, n: int) -> dict:
+    """The tuned configuration the table gives a sort of n keys."""
+    out = (C.c_int32 * 5)()
+    _check(load_library().turtle_tuning_lookup(dtype_code(dtype), int(track_index), int(n), out),
+           "tuning_lookup")
+    return {"form": out[0], "tile_shift": out[1], "geometry": out[2], "leaf_cut": out[3],
+            "grid_div": out[4]}
+
+
+def leaf_geometry(dtype, g: int) -> dict:
+    """Shared-memory sort geometry g: CTA threads, keys per thread, capacity,
+    size classes."""
+    out = (C.c_int32 * 4)()
+    if not load_library().turtle_leaf_geometry(dtype_code(dtype), int(g), out):
+        raise ValueError(f"no geometry {g}")
+    return {"threads": out[0], "items": out[1], "capacity": out[2], "classes": out[3]}
+
+
+def tuning_source() -> str:
+    return load_library().turtle_tuning_source().decode()
 
 
 class TurtleServer:

@@ -61,6 +61,13 @@ SIGNATURES = [
     ("turtle_debug_error_site", _I, [_P, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I)]),
     ("turtle_debug_yield_threshold", _I, [_P, C.c_int32]),
     ("turtle_debug_barrier_polls", _I, [_P, _I64]),
+    ("turtle_set_tuning", _I, [_P, _I]),
+    ("turtle_set_config", _I, [_P, _I, _I, _I, _I, _I]),
+    ("turtle_tuning_lookup", _I, [_I, _I, _I64, _P]),
+    ("turtle_tuning_multisort_geometry", _I, [_I, _I, _I64]),
+    ("turtle_tuning_source", C.c_char_p, []),
+    ("turtle_leaf_geometry", _I, [_I, _I, _P]),
+    ("turtle_debug_multisort_geometry", _I, [_I, _P, _P, _I64, _I64, _I, _P]),
     ("turtle_server_create", _I, [_I, _I64, _I, _I64, C.POINTER(_P)]),
     ("turtle_server_submit", _I, [_P, _I, _P, _P, _I64, C.POINTER(C.c_uint64)]),
     ("turtle_server_poll", _I, [_P, C.c_uint64, C.POINTER(_I)]),

@@ -40,7 +40,8 @@ def sources() -> list[Path]:
 
 def _compile(src: Path, verbose_ptxas: bool) -> Path:
     obj = BUILD / (src.stem + ".o")
-    deps = [src] + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list(INCLUDE.glob("*.h"))
+    deps = [src] + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list(CSRC.glob("*.inc")) + \
+        list(INCLUDE.glob("*.h"))
     if obj.exists() and all(obj.stat().st_mtime >= d.stat().st_mtime for d in deps):
         return obj
     cmd = [nvcc(), *ARCH, *NVFLAGS, "-c", str(src), "-o", str(obj)]

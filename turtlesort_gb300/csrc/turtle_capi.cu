@@ -20,6 +20,7 @@
 #include "turtle_device.cuh"
 #include "turtle_internal.h"
 #include "turtle_layout.cuh"
+#include "turtle_tuning.h"
 
 using turtle::DevBuffer;
 using turtle::WsLayout;
@@ -78,6 +79,11 @@ struct turtle_sorter {
   bool yielded = false;     // the partition yielded: those copies may be stale
   int leafYield = 0;        // test threshold for yields (0: default)
   long long barrierPolls = 0;  // test limit of the grid-barrier wait (0: default)
+  // launch configuration: the tuned table (default), the compile-time
+  // defaults, or one pinned configuration
+  bool tuning = true;
+  bool pinned = false;
+  turtle::TuneParams pin = {};
   // optional kernel timing: events around the two launches of each sort
   static constexpr int kRing = 64;
   bool timeKernels = false;
@@ -107,19 +113,35 @@ void free_graphs(turtle_sorter* s) {
   s->graphs.clear();
 }
 
+// The work lists are laid out for the smallest tile and leaf cut any
+// configuration of this sorter can use (table entries up to max_n, with and
+// without ids, and a pinned configuration).
 turtle_status alloc_workspace(turtle_sorter* s, long long extraLeaves) {
   turtle::vmm_free(&s->ws);
-  s->lay = make_layout(s->maxN, turtle::kernels_tile_elems(s->width),
-                       turtle::kernels_leaf_max(s->width), extraLeaves);
+  int ts0 = 0, lc0 = 0, ts1 = 0, lc1 = 0;
+  turtle::tune_layout_bounds(s->width, false, s->maxN, &ts0, &lc0);
+  turtle::tune_layout_bounds(s->width, true, s->maxN, &ts1, &lc1);
+  int ts = ts0 < ts1 ? ts0 : ts1, lc = lc0 < lc1 ? lc0 : lc1;
+  if (s->pinned) {
+    const turtle::TuneParams p = turtle::tune_sanitize(s->width, s->pin);
+    ts = p.tileShift < ts ? p.tileShift : ts;
+    lc = p.leafCut < lc ? p.leafCut : lc;
+  }
+  s->lay = make_layout(s->maxN, 1 << ts, lc, extraLeaves);
   TRY_CUDA(s, turtle::vmm_alloc(&s->ws, s->lay.bytes, s->device, false));
   return TURTLE_OK;
+}
+
+turtle::TuneParams pick_params(turtle_sorter* s, bool hasIdx, long long n) {
+  if (s->pinned) return s->pin;
+  return s->tuning ? turtle::tune_lookup(s->width, hasIdx, n) : turtle::tune_defaults(s->width, n);
 }
 
 turtle::SortArgs make_args(turtle_sorter* s, void* keys, int32_t* idx, const long long* offs,
                            long long num, long long n, int slices = 1) {
   turtle::SortArgs a = turtle::bind_args(keys, idx, s->keysB.ptr, (int*)s->idxB.ptr,
                                          (char*)s->ws.ptr, s->lay, offs, num, n, s->dtype,
-                                         s->pivotRule);
+                                         s->pivotRule, pick_params(s, idx != nullptr, n));
   a.slices = slices;
   a.leafYield = s->leafYield;
   a.barrierPolls = s->barrierPolls;
@@ -138,7 +160,9 @@ cudaError_t enqueue_persistent(turtle_sorter* s, const turtle::SortArgs& a, bool
   cudaEvent_t* ev = s->ev[s->timed % turtle_sorter::kRing];
   cudaError_t e = cudaSuccess;
   if (timing && (e = cudaEventRecord(ev[0], st)) != cudaSuccess) return e;
-  e = turtle::kernels_launch_persistent(s->width, hasIdx, a, s->grid[hasIdx ? 1 : 0], st,
+  const int full = s->grid[hasIdx ? 1 : 0];
+  const int grid = full / (a.gridDiv > 0 ? a.gridDiv : 1);
+  e = turtle::kernels_launch_persistent(s->width, hasIdx, a, grid > 0 ? grid : 1, st,
                                         timing ? ev[1] : nullptr,
                                         a.slices > 1 ? s->sliceEv : nullptr);
   if (e != cudaSuccess) return e;
@@ -402,11 +426,22 @@ turtle_status turtle_multisort_device(turtle_sorter* s, void* d_keys, int32_t* d
   if (arr_size < 2 || num_arrays == 0) return TURTLE_OK;
   cudaSetDevice(s->device);
   cudaStream_t cs = pick_stream(s, stream);
-  const int leafMax = turtle::kernels_leaf_max(s->width);
-  if (arr_size <= leafMax) {
+  // shared-memory geometry: the tuned one for this array length, if it holds
+  // the arrays, else the smallest geometry that does
+  int geom = s->tuning ? turtle::tune_multi_lookup(s->width, d_idx != nullptr, (int)arr_size) : -1;
+  int cap = 0;
+  if (geom >= 0) turtle::kernels_leaf_geometry(s->width, geom, nullptr, nullptr, &cap, nullptr);
+  if (geom < 0 || arr_size > cap) {
+    geom = -1;
+    for (int g : {turtle::kDefaultLeafGeometry, 2}) {
+      turtle::kernels_leaf_geometry(s->width, g, nullptr, nullptr, &cap, nullptr);
+      if (arr_size <= cap) { geom = g; break; }
+    }
+  }
+  if (geom >= 0) {
     TRY_CUDA(s, turtle::kernels_launch_multisort(s->width, d_idx != nullptr, d_keys, d_idx,
                                                  num_arrays, (int)arr_size, s->flip,
-                                                 turtle::dtype_fbits(s->dtype), cs));
+                                                 turtle::dtype_fbits(s->dtype), geom, cs));
     s->launches.fetch_add(1);
     std::memset(s->hctrl, 0, sizeof(turtle::Control));
     return TURTLE_OK;
@@ -647,6 +682,98 @@ turtle_status turtle_debug_barrier_polls(turtle_sorter* s, int64_t polls) {
   s->barrierPolls = polls;
   free_graphs(s);  // captured launches carry the old limit
   return TURTLE_OK;
+}
+
+turtle_status turtle_set_tuning(turtle_sorter* s, int enable) {
+  if (!s) return TURTLE_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->tuning = enable != 0;
+  free_graphs(s);  // captured launches carry the old configuration
+  return TURTLE_OK;
+}
+
+turtle_status turtle_set_config(turtle_sorter* s, int form, int tile_shift, int leaf_geometry,
+                                int leaf_cut, int grid_div) {
+  if (!s) return TURTLE_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(s->mu);
+  free_graphs(s);
+  if (form < 0) {
+    s->pinned = false;
+    return TURTLE_OK;
+  }
+  if ((form != turtle::kRuleSampled && form != turtle::kRuleTwoLevel) ||
+      tile_shift < turtle::kMinTileShift || tile_shift > turtle::kMaxTileShift ||
+      leaf_geometry < 0 || leaf_geometry >= turtle::kLeafGeometries ||
+      (grid_div != 1 && grid_div != 2 && grid_div != 4))
+    return TURTLE_ERR_INVALID_ARGUMENT;
+  int cap = 0;
+  turtle::kernels_leaf_geometry(s->width, leaf_geometry, nullptr, nullptr, &cap, nullptr);
+  if (leaf_cut < turtle::kMinLeafCut || leaf_cut > cap) return TURTLE_ERR_INVALID_ARGUMENT;
+  turtle::TuneParams p;
+  p.form = form;
+  p.tileShift = tile_shift;
+  p.leafGeom = leaf_geometry;
+  p.leafCut = leaf_cut;
+  p.gridDiv = grid_div;
+  const bool relayout = tile_shift < s->lay.tileShift || leaf_cut < s->lay.leafMax;
+  s->pin = p;
+  s->pinned = true;
+  if (relayout) {
+    cudaSetDevice(s->device);
+    if (cudaDeviceSynchronize() != cudaSuccess) return from_cuda(s, cudaGetLastError());
+    return alloc_workspace(s, 0);
+  }
+  return TURTLE_OK;
+}
+
+turtle_status turtle_tuning_lookup(turtle_dtype dtype, int track_index, int64_t n,
+                                   int32_t* out5) {
+  const int w = turtle::dtype_width(dtype);
+  if (!w || !out5 || n < 0) return TURTLE_ERR_INVALID_ARGUMENT;
+  const turtle::TuneParams p = turtle::tune_lookup(w, track_index != 0, n);
+  out5[0] = p.form;
+  out5[1] = p.tileShift;
+  out5[2] = p.leafGeom;
+  out5[3] = p.leafCut;
+  out5[4] = p.gridDiv;
+  return TURTLE_OK;
+}
+
+int turtle_tuning_multisort_geometry(turtle_dtype dtype, int track_index, int64_t arr_size) {
+  const int w = turtle::dtype_width(dtype);
+  if (!w || arr_size < 0 || arr_size > (1LL << 30)) return -1;
+  return turtle::tune_multi_lookup(w, track_index != 0, (int)arr_size);
+}
+
+const char* turtle_tuning_source(void) { return turtle::tune_source(); }
+
+turtle_status turtle_debug_multisort_geometry(turtle_dtype dtype, void* d_keys, int32_t* d_idx,
+                                              int64_t arr_size, int64_t num_arrays, int geometry,
+                                              void* stream) {
+  const int w = turtle::dtype_width(dtype);
+  if (!w || arr_size < 0 || num_arrays < 0 || geometry < 0 ||
+      geometry >= turtle::kLeafGeometries || (!d_keys && arr_size * num_arrays > 0))
+    return TURTLE_ERR_INVALID_ARGUMENT;
+  int cap = 0;
+  turtle::kernels_leaf_geometry(w, geometry, nullptr, nullptr, &cap, nullptr);
+  if (arr_size > cap) return TURTLE_ERR_TOO_LARGE;
+  if (arr_size < 2 || num_arrays == 0) return TURTLE_OK;
+  int dev = 0, grid = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return from_cuda(nullptr, cudaGetLastError());
+  cudaError_t e = turtle::kernels_prepare(w, d_idx != nullptr, dev, &grid);
+  if (e == cudaSuccess)
+    e = turtle::kernels_launch_multisort(w, d_idx != nullptr, d_keys, d_idx, num_arrays,
+                                         (int)arr_size, dtype_flip(dtype),
+                                         turtle::dtype_fbits(dtype), geometry,
+                                         (cudaStream_t)stream);
+  return from_cuda(nullptr, e);
+}
+
+int turtle_leaf_geometry(turtle_dtype dtype, int geometry, int32_t* out4) {
+  const int w = turtle::dtype_width(dtype);
+  if (!w || !out4 || geometry < 0 || geometry >= turtle::kLeafGeometries) return 0;
+  turtle::kernels_leaf_geometry(w, geometry, &out4[0], &out4[1], &out4[2], &out4[3]);
+  return 1;
 }
 
 const char* turtle_version(void) { return "turtle-gb300 0.1 (sm_103a)"; }

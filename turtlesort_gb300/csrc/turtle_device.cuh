@@ -34,8 +34,7 @@ constexpr int kMinBlocks = TURTLE_PART_BLOCKS; // resident partition CTAs per SM
 #define TURTLE_PART_TILE 2048
 #endif
 constexpr int kPartTile = TURTLE_PART_TILE;  // partition tile (keys), a power of two
-constexpr int kLThreads = 512;           // CTA size of the leaf / batched kernels
-constexpr int kLWarps = kLThreads / 32;
+constexpr int kLThreads = 512;           // CTA size of the default leaf / batched geometry
 constexpr int kFillChunk = 1 << 16;      // pivot-run fill work unit (elements)
 #ifndef TURTLE_DEPTH_SWITCH
 #define TURTLE_DEPTH_SWITCH 48
@@ -46,7 +45,6 @@ constexpr int kMaxLevels = 4096;         // hard cap on partition levels
 constexpr int kSamples = 31;             // evenly spaced pivot samples (one-level sampled rule)
 constexpr int kWideSamples = 63;         // pivot samples of a segment in two-level passes
 constexpr int kRow = 32;                 // per-tile row: 32 class counts / offsets / sample keys
-constexpr int kLeafClasses = 10;         // group sizes 1, 2, 4, ..., 512 threads
 constexpr int kMaxSlices = 8;
 constexpr int kSmallPlanTiles = 64;      // segments this small are planned by one warp            // leaf phase split by position (one launch each)
 constexpr long long kSpinLimit = 40000000LL;  // bounded barrier spin iterations
@@ -67,13 +65,32 @@ template <> struct KeyCfg<uint16_t> { using KT = uint32_t; static constexpr int 
 template <> struct KeyCfg<uint32_t> { using KT = uint32_t; static constexpr int kItems = 8, kLItems = 16; };
 template <> struct KeyCfg<uint64_t> { using KT = uint64_t; static constexpr int kItems = 4, kLItems = 8; };
 
+// Geometries of the shared-memory sort (leaf kernel and MultiSort kernel),
+// selected at run time: CTA size x keys per thread.  kLItems (16 for keys of
+// up to 32 bits, 8 for 64-bit keys) is the size of the register network;
+// geometry 3 halves it, so an array gets twice the threads.
+//   0: 256 threads x kLItems      (capacity 4096 / 2048)
+//   1: 512 threads x kLItems      (capacity 8192 / 4096, the default)
+//   2: 1024 threads x kLItems     (capacity 16384 / 8192)
+//   3: 512 threads x kLItems / 2  (capacity 4096 / 2048)
+constexpr int kLeafGeometries = 4;
+constexpr int kDefaultLeafGeometry = 1;
+template <typename U, int kV>
+struct LeafGeom {
+  static constexpr int kThreads = kV == 0 ? 256 : kV == 2 ? 1024 : 512;
+  static constexpr int kItems = kV == 3 ? KeyCfg<U>::kLItems / 2 : KeyCfg<U>::kLItems;
+  static constexpr int kMax = kThreads * kItems;
+  static constexpr int kBlocks = 1024 / kThreads;  // resident CTAs per SM at 64 registers
+  static constexpr int kClasses = kV == 0 ? 9 : kV == 2 ? 11 : 10;  // groups of 1 .. kThreads threads
+};
+
 template <typename U>
 struct Geom {
   using KT = typename KeyCfg<U>::KT;
   static constexpr int kItems = KeyCfg<U>::kItems;
   static constexpr int kLItems = KeyCfg<U>::kLItems;
   static constexpr int kTile = kPartTile;               // partition tile
-  static constexpr int kLeafMax = kLThreads * kLItems;  // shared-memory sort capacity
+  static constexpr int kLeafMax = kLThreads * kLItems;  // capacity of the default leaf geometry
   static constexpr int kWarpChunk = 32 * kItems;        // elements per warp chunk
 };
 
@@ -195,6 +212,12 @@ struct SortArgs {
   int samples;               // pivot samples per segment: 3 (reference rule, one-level
                              // passes) or kWideSamples (sampled rule, two-level passes)
   long long barrierPolls;    // > 0: grid-barrier poll limit (testing the timeout), else kSpinLimit
+  int tileShift;             // partition tile = 1 << tileShift keys (10..12)
+  int leafCut;               // segments of at most leafCut keys become leaves
+  int leafItems;             // keys per thread of the leaf sort (size classes)
+  int leafClasses;           // leaf size classes: thread groups of 1, 2, ..., 2^(leafClasses-1)
+  int leafVariant;           // geometry of the leaf kernel (see kernels_leaf_geometry)
+  int gridDiv;               // the partition kernel runs on (resident CTAs) / gridDiv CTAs
   Control* ctrl;
 };
 
@@ -585,10 +608,16 @@ __device__ __forceinline__ void cex(typename LW::W& a, typename LW::W& b) {
 // comparators are written out so every index is a literal and the words stay
 // in registers.
 template <class LW, int N> struct Network;
+#define TURTLE_C(x, y) cex<LW>(v[x], v[y]);
+template <class LW>
+struct Network<LW, 4> {
+  __device__ __forceinline__ static void sort(typename LW::W* v) {
+    TURTLE_C(0,1) TURTLE_C(2,3) TURTLE_C(0,2) TURTLE_C(1,3) TURTLE_C(1,2)
+  }
+};
 template <class LW>
 struct Network<LW, 8> {
   __device__ __forceinline__ static void sort(typename LW::W* v) {
-#define TURTLE_C(x, y) cex<LW>(v[x], v[y]);
     TURTLE_C(0,1) TURTLE_C(2,3) TURTLE_C(4,5) TURTLE_C(6,7) TURTLE_C(0,2) TURTLE_C(1,3)
     TURTLE_C(4,6) TURTLE_C(5,7) TURTLE_C(1,2) TURTLE_C(5,6) TURTLE_C(0,4) TURTLE_C(1,5)
     TURTLE_C(2,6) TURTLE_C(3,7) TURTLE_C(2,4) TURTLE_C(3,5) TURTLE_C(1,2) TURTLE_C(3,4)
@@ -691,10 +720,9 @@ __device__ __forceinline__ void block_sort_words(typename LW::W* sw, int P, int 
 }
 
 // Size class of a leaf: the smallest power-of-two thread group whose
-// registers hold it (class c uses P = 1 << c threads).
-template <int kItems>
-__device__ __forceinline__ int leaf_class(int n) {
-  int p = (n + kItems - 1) / kItems;
+// registers hold it (class c uses P = 1 << c threads of `items` keys each).
+__device__ __forceinline__ int leaf_class(int n, int items) {
+  const int p = (n + items - 1) / items;
   int c = 0;
   while ((1 << c) < p) ++c;
   return c;

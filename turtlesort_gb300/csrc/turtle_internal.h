@@ -21,9 +21,12 @@ cudaError_t kernels_launch_persistent(int width, bool hasIdx, const SortArgs& a,
                                       const cudaEvent_t* sliceDone = nullptr);
 cudaError_t kernels_launch_multisort(int width, bool hasIdx, void* keys, int* idx,
                                      long long numArrays, int arrSize, unsigned long long flip,
-                                     int fbits, cudaStream_t stream);
+                                     int fbits, int geometry, cudaStream_t stream);
 int kernels_tile_elems(int width);
 int kernels_leaf_max(int width);
+// Geometry g (0..3) of the leaf / MultiSort kernels for keys of `width` bytes.
+void kernels_leaf_geometry(int width, int g, int* threads, int* items, int* capacity,
+                           int* classes);
 
 // ---- device buffers on the driver VMM API (turtle_vmm.cu) ----
 // Replaces TurtleBuffer::Buffer (turtle-buffer.cuh:7-100) and

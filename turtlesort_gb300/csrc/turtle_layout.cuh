@@ -7,6 +7,8 @@
 
 #include "../../include/turtle_gb300.h"
 #include "turtle_device.cuh"
+#include "turtle_internal.h"
+#include "turtle_tuning.h"
 
 namespace turtle {
 
@@ -20,6 +22,8 @@ struct WsLayout {
   size_t offLeaves = 0, offLeavesSorted = 0, offFills = 0, bytes = 0;
   bool hasCls = false;   // per-key class bytes (two-level passes need them)
   size_t offCls = 0;
+  int tileShift = 11;    // the smallest partition tile the lists are sized for
+  int leafMax = 0;       // the smallest leaf cut the lists are sized for
 };
 
 // classBytes: room for the per-key class bytes of two-level passes (without
@@ -27,6 +31,9 @@ struct WsLayout {
 inline WsLayout make_layout(long long maxN, int tile, int leafMax, long long extraLeaves,
                             bool classBytes = true) {
   WsLayout L;
+  L.tileShift = 0;
+  while ((1 << L.tileShift) < tile) ++L.tileShift;
+  L.leafMax = leafMax;
   // segments of one level are disjoint and longer than leafMax
   const long long segCap = maxN / leafMax + 66;
   const long long tileCap = maxN / tile + 2 * segCap + 64;
@@ -101,9 +108,12 @@ inline int rule_samples(int rule) {
   return rule == kRuleReference ? 3 : rule == kRuleTwoLevel ? kWideSamples : kSamples;
 }
 
+// Launch configuration tp (see turtle_tuning.h) decides the pass form under
+// kRuleAuto, the tile, the leaf geometry and cut; it is clamped to what the
+// work lists were laid out for.
 inline SortArgs bind_args(void* keys, int* idx, void* keysB, int* idxB, char* ws, const WsLayout& L,
                           const long long* offs, long long num, long long n, int dtype,
-                          int rule = kRuleAuto) {
+                          int rule, TuneParams tp) {
   SortArgs a;
   std::memset(&a, 0, sizeof(a));
   a.keysA = keys;
@@ -133,12 +143,27 @@ inline SortArgs bind_args(void* keys, int* idx, void* keysB, int* idxB, char* ws
   a.fillCap = L.fillCap;
   a.planCap = L.planCap;
   a.ctrl = (Control*)(ws + L.offCtrl);
-  if (rule == kRuleAuto) rule = n >= kAutoTwoLevelKeys ? kRuleTwoLevel : kRuleSampled;
+  const int width = dtype_width(dtype);
+  tp = tune_sanitize(width, tp);
+  int cap = 0;
+  kernels_leaf_geometry(width, tp.leafGeom, nullptr, nullptr, &cap, nullptr);
+  if (L.leafMax > cap) {  // the lists need longer leaves than this geometry holds
+    tp.leafGeom = kDefaultLeafGeometry;
+    kernels_leaf_geometry(width, tp.leafGeom, nullptr, nullptr, &cap, nullptr);
+  }
+  if (tp.leafCut < L.leafMax) tp.leafCut = L.leafMax < cap ? L.leafMax : cap;
+  if (tp.tileShift < L.tileShift) tp.tileShift = L.tileShift;
+  if (rule == kRuleAuto) rule = tp.form;
   if (rule == kRuleTwoLevel && !L.hasCls) rule = kRuleSampled;
   a.cls = L.hasCls ? (unsigned char*)(ws + L.offCls) : nullptr;
   a.samples = rule_samples(rule);
   a.slices = 1;
   a.leafYield = 0;
+  a.tileShift = tp.tileShift;
+  a.leafCut = tp.leafCut;
+  a.leafVariant = tp.leafGeom;
+  a.gridDiv = tp.gridDiv;
+  kernels_leaf_geometry(width, tp.leafGeom, nullptr, &a.leafItems, nullptr, &a.leafClasses);
   return a;
 }
 

@@ -103,8 +103,9 @@ struct turtle_server {
 namespace {
 
 size_t batch_bytes(int width, bool hasIdx, long long total, long long num, turtle::WsLayout* layOut) {
-  const turtle::WsLayout lay = turtle::make_layout(std::max(total, 2LL), turtle::kernels_tile_elems(width),
-                                                   turtle::kernels_leaf_max(width), num);
+  int ts = 0, lc = 0;  // laid out for the configuration the table gives this batch
+  turtle::tune_layout_bounds(width, hasIdx, std::max(total, 2LL), &ts, &lc);
+  const turtle::WsLayout lay = turtle::make_layout(std::max(total, 2LL), 1 << ts, lc, num);
   size_t b = 0;
   const size_t kb = turtle::align_up((size_t)total * width + 16, 256);
   const size_t ib = hasIdx ? turtle::align_up((size_t)total * 4 + 16, 256) : 0;
@@ -157,11 +158,13 @@ turtle_status launch_batch(turtle_server* s, Batch* b) {
   cudaEventRecord(sl.inDone, s->sIn);
   // sort
   b->args = turtle::bind_args(keys, idx, keysB, idxB, ws, b->lay, offs, num, b->total,
-                              b->dtype);
+                              b->dtype, turtle::kRuleAuto,
+                              turtle::tune_lookup(b->width, b->hasIdx, b->total));
   cudaStreamWaitEvent(s->sSort, sl.inDone, 0);
   cudaMemsetAsync(b->args.ctrl, 0, sizeof(turtle::Control), s->sSort);
   e = turtle::kernels_launch_persistent(b->width, b->hasIdx, b->args,
-                                        s->grid[b->width][b->hasIdx ? 1 : 0], s->sSort);
+                                        std::max(1, s->grid[b->width][b->hasIdx ? 1 : 0] / b->args.gridDiv),
+                                        s->sSort);
   if (e != cudaSuccess) { cudaGetLastError(); return TURTLE_ERR_CUDA; }
   cudaMemcpyAsync(sl.hCtrl, b->args.ctrl, sizeof(turtle::Control), cudaMemcpyDeviceToHost,
                   s->sSort);
@@ -194,9 +197,9 @@ turtle_status finish_batch(turtle_server* s, Batch* b) {
       break;
     }
     b->args.resume = 1;
-    cudaError_t e = turtle::kernels_launch_persistent(b->width, b->hasIdx, b->args,
-                                                      s->grid[b->width][b->hasIdx ? 1 : 0],
-                                                      s->sSort);
+    cudaError_t e = turtle::kernels_launch_persistent(
+        b->width, b->hasIdx, b->args,
+        std::max(1, s->grid[b->width][b->hasIdx ? 1 : 0] / b->args.gridDiv), s->sSort);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(sl.hCtrl, b->args.ctrl, sizeof(turtle::Control),
                           cudaMemcpyDeviceToHost, s->sSort);

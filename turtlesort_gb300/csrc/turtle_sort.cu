@@ -64,10 +64,6 @@ struct Persist {
   using G = Geom<U>;
   using KT = typename G::KT;
   static constexpr int kItems = G::kItems;
-  static constexpr int kTile = G::kTile;
-  static constexpr int kTileShift = ilog2(kTile);
-  static_assert((1 << kTileShift) == kTile, "tiles are a power of two");
-  static constexpr int kLeafMax = G::kLeafMax;
   static constexpr int kWCH = G::kWarpChunk;
   static_assert(kWCH == 32 * kItems && kWCH <= 256, "stage slots are 8-bit");
   static_assert(kItems <= 8, "per-lane class counters are 4-bit");
@@ -137,19 +133,29 @@ struct Persist {
     WidePivots<KT> wpiv;
   };
 
+};
+
+// Shared memory of a leaf / MultiSort CTA of geometry kV.
+template <typename U, bool kIdx, int kV>
+struct LeafCfg {
+  using LG = LeafGeom<U, kV>;
+  using KT = typename KeyCfg<U>::KT;
+  static constexpr int kThreads = LG::kThreads, kItems = LG::kItems, kMax = LG::kMax;
+  static constexpr int kWarps = kThreads / 32;
   using LW = LeafWord<U, kIdx>;
   using LWord = typename LW::W;
-  // word arrays of the shared-memory sort: full-range words, or (leaves)
-  // range-packed 32-bit words or, for 64-bit keys with ids, 64-bit words
-  static constexpr size_t kLeafWordBytes =
-      sizeof(LWord) * (size_t)word_slots<LWord>(G::kLeafMax) > 8 * (size_t)word_slots<uint64_t>(G::kLeafMax)
-          ? sizeof(LWord) * (size_t)word_slots<LWord>(G::kLeafMax)
-          : 8 * (size_t)word_slots<uint64_t>(G::kLeafMax);
-  struct LeafSmem {  // leaf / batched CTA
-    alignas(16) unsigned char wbytes[kLeafWordBytes];  // packed key (+ position) words
-    int idx[kIdx ? G::kLeafMax + 8 : 4];                // ids by position
-    KT gmin[kLWarps], gmax[kLWarps];                    // per-warp key range of the loaded leaves
-    KT glo[kLThreads];                                  // smallest key of each group's leaf
+  static constexpr size_t cmax(size_t x, size_t y) { return x > y ? x : y; }
+  // the word buffer holds the full-range words, the range-packed 32-bit words,
+  // for 64-bit keys with ids 64-bit words, and the raw keys while they load
+  static constexpr size_t kWordBytes = cmax(
+      cmax(sizeof(LWord) * (size_t)word_slots<LWord>(kMax), 4 * (size_t)word_slots<uint32_t>(kMax)),
+      cmax((sizeof(U) == 8 && kIdx) ? 8 * (size_t)word_slots<uint64_t>(kMax) : 0,
+           sizeof(KT) * (size_t)kMax));
+  struct Smem {
+    alignas(16) unsigned char wbytes[kWordBytes];  // packed key (+ position) words
+    int idx[kIdx ? kMax + 8 : 4];                   // ids by position
+    KT gmin[kWarps], gmax[kWarps];                  // per-warp key range of the loaded leaves
+    KT glo[kThreads];                               // smallest key of each group's leaf
     int item;
     int classOff[16];
     int classItems[16];
@@ -178,9 +184,9 @@ template <typename U, bool kIdx>
 constexpr size_t persist_smem_bytes() {
   return sizeof(typename Persist<U, kIdx>::Smem);
 }
-template <typename U, bool kIdx>
+template <typename U, bool kIdx, int kV>
 constexpr size_t leaf_smem_bytes() {
-  return sizeof(typename Persist<U, kIdx>::LeafSmem);
+  return sizeof(typename LeafCfg<U, kIdx, kV>::Smem);
 }
 
 // ---------------------------------------------------------------------------
@@ -261,9 +267,8 @@ __device__ __forceinline__ void segment_pivots_warp(const SegDesc* sd, const U* 
   piv[2] = __shfl_sync(kFull, v, l3);
 }
 
-template <int kTile>
-__device__ __forceinline__ long long tiles_of(long long start, long long n) {
-  return (start + n - 1) / kTile - start / kTile + 1;
+__device__ __forceinline__ long long tiles_of(long long start, long long n, int shift) {
+  return ((start + n - 1) >> shift) - (start >> shift) + 1;
 }
 
 // Allocate a next-level segment (tile range allocated with the same 64-bit
@@ -271,10 +276,9 @@ __device__ __forceinline__ long long tiles_of(long long start, long long n) {
 // index or -1 on overflow.  The caller writes the tile descriptors.  With
 // smallPlans, a segment of at most kSmallPlanTiles tiles goes to the list of
 // segments planned by one warp instead of getting CTA plan items.
-template <int kTile>
 __device__ int alloc_segment(const SortArgs& a, int par, long long start, long long n,
                              int* tbOut, int* ntOut, bool smallPlans) {
-  const long long nt = tiles_of<kTile>(start, n);
+  const long long nt = tiles_of(start, n, a.tileShift);
   const unsigned long long old =
       atomicAdd(&a.ctrl->segTile[par], (1ull << 32) | (unsigned long long)nt);
   const int si = (int)(old >> 32);
@@ -308,16 +312,17 @@ __device__ int alloc_segment(const SortArgs& a, int par, long long start, long l
 }
 
 // Tile descriptors of a segment, written by threads [t0, t0+stride) of a group.
-template <int kTile>
 __device__ void write_tiles(const SortArgs& a, int par, int si, int tb, int nt, long long start,
                             long long n, int t0, int stride) {
-  const long long first = start / kTile;
+  const int sh = a.tileShift;
+  const long long tile = 1LL << sh;
+  const long long first = start >> sh;
   const long long end = start + n;
   for (int i = t0; i < nt; i += stride) {
-    const long long abs0 = (first + i) * (long long)kTile;
+    const long long abs0 = (first + i) << sh;
     TileDesc d;
     d.lo = abs0 > start ? abs0 : start;
-    d.hi = (abs0 + kTile) < end ? (abs0 + kTile) : end;
+    d.hi = (abs0 + tile) < end ? (abs0 + tile) : end;
     d.seg = si;
     d.pad = 0;
     a.tiles[par][tb + i] = d;
@@ -358,16 +363,16 @@ __device__ void push_fill(const SortArgs& a, long long start, long long n, unsig
 // Route one input array at init: nothing, leaf, or level-0 segment (with its
 // pivot candidates, unless the caller reads them; its tiles are written when
 // writeTiles).
-template <typename U, int kTile, int kLeafMax>
+template <typename U>
 __device__ void route_input(const SortArgs& a, long long start, long long n, bool writeTiles,
                             int* siOut, int* tbOut, int* ntOut, bool samples = true) {
   *siOut = -1;
   *tbOut = 0;
   *ntOut = 0;
   if (n <= 1) return;
-  if (n <= kLeafMax) { push_leaf(a, start, n, 0); return; }
+  if (n <= a.leafCut) { push_leaf(a, start, n, 0); return; }
   int tb = 0, nt = 0;
-  const int si = alloc_segment<kTile>(a, 0, start, n, &tb, &nt, true);
+  const int si = alloc_segment(a, 0, start, n, &tb, &nt, true);
   if (si < 0) return;
   using KT = typename KeyCfg<U>::KT;
   const U* src = (const U*)a.keysA;
@@ -376,7 +381,7 @@ __device__ void route_input(const SortArgs& a, long long start, long long n, boo
   sd->nsamp = a.samples;
   for (int i = 0; samples && i < a.samples; ++i)
     sd->samp[i] = (unsigned long long)kload<U, KT>(src, sample_pos(start, n, i, a.samples), flip);
-  if (writeTiles) write_tiles<kTile>(a, 0, si, tb, nt, start, n, 0, 1);
+  if (writeTiles) write_tiles(a, 0, si, tb, nt, start, n, 0, 1);
   *siOut = si; *tbOut = tb; *ntOut = nt;
 }
 
@@ -489,7 +494,8 @@ __device__ __forceinline__ void count_tile_warp(const SortArgs& a, int level, in
                                                 unsigned& phases, int& accSeg, int& accCnt) {
   using P = Persist<U, kIdx>;
   using KT = typename P::KT;
-  constexpr int kItems = P::kItems, kWCH = P::kWCH, kShift = P::kTileShift;
+  constexpr int kItems = P::kItems, kWCH = P::kWCH;
+  const int kShift = a.tileShift;
   constexpr int kR = P::kCountRing, kCB = P::kChunkBytes;
   const int par = level & 1;
   const int lane = threadIdx.x & 31;
@@ -653,7 +659,7 @@ __device__ __noinline__ void plan_item(const SortArgs& a, int level, int item,
                                        typename Persist<U, kIdx>::Smem& sm) {
   using P = Persist<U, kIdx>;
   using KT = typename P::KT;
-  constexpr int kTile = P::kTile, kLeafMax = P::kLeafMax;
+  const int kLeafMax = a.leafCut;
   const int par = level & 1;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int seg = __ldcg(&a.planSeg[par][item]);
@@ -752,7 +758,7 @@ __device__ __noinline__ void plan_item(const SortArgs& a, int level, int item,
           push_leaf(a, pos, m, dstIsA ? 0 : 1);
         } else {
           int tb = 0, ntc = 0;
-          si = alloc_segment<kTile>(a, nextPar, pos, m, &tb, &ntc, true);
+          si = alloc_segment(a, nextPar, pos, m, &tb, &ntc, true);
           sm.childTb[ci] = tb;
           sm.childNt[ci] = si >= 0 ? ntc : 0;
           sm.childStart[ci] = pos;
@@ -770,7 +776,7 @@ __device__ __noinline__ void plan_item(const SortArgs& a, int level, int item,
   __syncthreads();
   for (int ci = 0; ci < 4; ++ci) {
     if (sm.childSeg[ci] >= 0)
-      write_tiles<kTile>(a, nextPar, sm.childSeg[ci], sm.childTb[ci], sm.childNt[ci],
+      write_tiles(a, nextPar, sm.childSeg[ci], sm.childTb[ci], sm.childNt[ci],
                          sm.childStart[ci], sm.childN[ci], tid, kThreads);
   }
   __syncthreads();
@@ -784,7 +790,7 @@ template <typename U, bool kIdx>
 __device__ __noinline__ void plan_small_warp(const SortArgs& a, int level, int seg) {
   using P = Persist<U, kIdx>;
   using KT = typename P::KT;
-  constexpr int kTile = P::kTile, kLeafMax = P::kLeafMax;
+  const int kLeafMax = a.leafCut;
   static_assert(kSmallPlanTiles == 64, "two tiles per lane");
   const int par = level & 1;
   const int lane = threadIdx.x & 31;
@@ -835,7 +841,7 @@ __device__ __noinline__ void plan_small_warp(const SortArgs& a, int level, int s
     } else {
       if (m > 1 || (m == 1 && !dstIsA)) {
         if (m <= kLeafMax) push_leaf(a, pos, m, dstIsA ? 0 : 1);
-        else si = alloc_segment<kTile>(a, nextPar, pos, m, &tb, &ntc, true);
+        else si = alloc_segment(a, nextPar, pos, m, &tb, &ntc, true);
       }
       sdp->childSeg[c >> 1] = si;
     }
@@ -853,7 +859,7 @@ __device__ __noinline__ void plan_small_warp(const SortArgs& a, int level, int s
       const int cnt2 = __shfl_sync(kFull, ntc, 2 * ci);
       const long long cs = __shfl_sync(kFull, pos, 2 * ci);
       const long long cn = __shfl_sync(kFull, m, 2 * ci);
-      write_tiles<kTile>(a, nextPar, s, ctb, cnt2, cs, cn, lane, 32);
+      write_tiles(a, nextPar, s, ctb, cnt2, cs, cn, lane, 32);
     }
   }
   __syncwarp();
@@ -879,7 +885,8 @@ __device__ __forceinline__ void scatter_tile_warp(const SortArgs& a, int level, 
                                                   unsigned& phases) {
   using P = Persist<U, kIdx>;
   using KT = typename P::KT;
-  constexpr int kItems = P::kItems, kWCH = P::kWCH, kShift = P::kTileShift;
+  constexpr int kItems = P::kItems, kWCH = P::kWCH;
+  const int kShift = a.tileShift;
   const int par = level & 1;
   const KT flip = (KT)a.flip;
   const int lane = threadIdx.x & 31;
@@ -1076,7 +1083,7 @@ __device__ __forceinline__ int leaf_slice(long long start, long long n, int slic
 // block.  Uses 2 grid barriers; returns false on error.
 template <typename U, bool kIdx>
 __device__ __noinline__ bool leaf_bucket(const SortArgs& a, typename Persist<U, kIdx>::Smem& sm) {
-  constexpr int kItems = Geom<U>::kLItems;
+  const int items = a.leafItems, classes = a.leafClasses;
   constexpr int kB = kMaxSlices * 16;
   Control* c = a.ctrl;
   const long long polls = a.barrierPolls > 0 ? a.barrierPolls : kSpinLimit;
@@ -1091,7 +1098,7 @@ __device__ __noinline__ bool leaf_bucket(const SortArgs& a, typename Persist<U, 
   __syncthreads();
   for (int i = blockIdx.x * kThreads + tid; i < nl; i += gridDim.x * kThreads) {
     const LeafDesc d = a.leaves[i];
-    atomicAdd(&sm.classItems[leaf_slice(d.start, a.n, S) * 16 + leaf_class<kItems>(d.n)], 1);
+    atomicAdd(&sm.classItems[leaf_slice(d.start, a.n, S) * 16 + leaf_class(d.n, items)], 1);
   }
   __syncthreads();
   for (int b = tid; b < S * 16; b += kThreads)
@@ -1102,7 +1109,7 @@ __device__ __noinline__ bool leaf_bucket(const SortArgs& a, typename Persist<U, 
   if (tid == 0) {
     int acc = 0;
     for (int s = 0; s < S; ++s) {
-      for (int k = kLeafClasses - 1; k >= 0; --k) {
+      for (int k = classes - 1; k >= 0; --k) {
         sm.classOff[s * 16 + k] = acc;
         acc += ld_acquire_int(&c->classCount[s * 16 + k]);
       }
@@ -1111,15 +1118,15 @@ __device__ __noinline__ bool leaf_bucket(const SortArgs& a, typename Persist<U, 
   __syncthreads();
   for (int i = blockIdx.x * kThreads + tid; i < nl; i += gridDim.x * kThreads) {
     const LeafDesc d = a.leaves[i];
-    const int b = leaf_slice(d.start, a.n, S) * 16 + leaf_class<kItems>(d.n);
+    const int b = leaf_slice(d.start, a.n, S) * 16 + leaf_class(d.n, items);
     const int pos = sm.classOff[b] + atomicAdd(&c->classFill[b], 1);
     a.leavesSorted[pos] = d;
   }
   if (blockIdx.x == 0 && tid == 0) {
     for (int s = 0; s < S; ++s) {
       int acc = 0;
-      for (int k = kLeafClasses - 1; k >= 0; --k) {
-        const int groups = kLThreads >> k;
+      for (int k = classes - 1; k >= 0; --k) {
+        const int groups = (1 << (classes - 1)) >> k;
         const int cnt = ld_acquire_int(&c->classCount[s * 16 + k]);
         c->classItemsG[s * 16 + k] = acc;  // first item of class k in slice s
         c->classOffG[s * 16 + k] = sm.classOff[s * 16 + k];
@@ -1177,7 +1184,7 @@ __device__ __forceinline__ void stream_tiles(const SortArgs& a, int level, int n
 template <typename U, bool kIdx, bool kWide>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(SortArgs a) {
   using P = Persist<U, kIdx>;
-  constexpr int kTile = P::kTile, kLeafMax = P::kLeafMax;
+  const int kLeafMax = a.leafCut;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   typename P::Smem& sm = *reinterpret_cast<typename P::Smem*>(smem_raw);
   Control* c = a.ctrl;
@@ -1209,7 +1216,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
     if (blockIdx.x == 0) {
       if (tid == 0) {
         int si, tb, nt;
-        route_input<U, kTile, kLeafMax>(a, 0, a.n, false, &si, &tb, &nt, false);
+        route_input<U>(a, 0, a.n, false, &si, &tb, &nt, false);
         sm.childSeg[0] = si;
         sm.childTb[0] = tb;
         sm.childNt[0] = nt;
@@ -1219,7 +1226,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
         a.segs[0][sm.childSeg[0]].samp[tid] = (unsigned long long)kload<U, typename P::KT>(
             (const U*)a.keysA, sample_pos(0, a.n, tid, a.samples), (typename P::KT)a.flip);
       if (sm.childSeg[0] >= 0)
-        write_tiles<kTile>(a, 0, sm.childSeg[0], sm.childTb[0], sm.childNt[0], 0, a.n, tid,
+        write_tiles(a, 0, sm.childSeg[0], sm.childTb[0], sm.childNt[0], 0, a.n, tid,
                            kThreads);
     }
   } else {
@@ -1227,7 +1234,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
          i += (long long)gridDim.x * kThreads) {
       const long long s = a.offsets[i], e = a.offsets[i + 1];
       int si, tb, nt;
-      route_input<U, kTile, kLeafMax>(a, s, e - s, true, &si, &tb, &nt);
+      route_input<U>(a, s, e - s, true, &si, &tb, &nt);
     }
   }
   if (!grid_barrier(c, polls)) return;
@@ -1338,14 +1345,15 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_sort_kernel(S
 // slots it wrote; the group's smallest key is `lo`.  What the output needs
 // after the sort (the leaf descriptor, lo) is reloaded then, which keeps the
 // sort within the register budget.
-template <typename U, bool kIdx, class LW>
+template <typename U, bool kIdx, int kV, class LW>
 __device__ __forceinline__ void leaf_words_sort(const SortArgs& a,
-                                                typename Persist<U, kIdx>::LeafSmem& sm, int P,
+                                                typename LeafCfg<U, kIdx, kV>::Smem& sm, int P,
                                                 int li, int last,
-                                                typename Persist<U, kIdx>::KT lo) {
-  using KT = typename Persist<U, kIdx>::KT;
+                                                typename KeyCfg<U>::KT lo) {
+  using KT = typename KeyCfg<U>::KT;
   using W = typename LW::W;
-  constexpr int kItems = Geom<U>::kLItems;
+  constexpr int kItems = LeafCfg<U, kIdx, kV>::kItems;
+  constexpr int kLT = LeafCfg<U, kIdx, kV>::kThreads;
   const int tid = threadIdx.x;
   const int g = tid / P, q = tid & (P - 1);
   const int n = li < last ? __ldcg(&a.leavesSorted[li].n) : 0;
@@ -1365,7 +1373,7 @@ __device__ __forceinline__ void leaf_words_sort(const SortArgs& a,
   }
   if (q == 0) sm.glo[g] = lo;
   __syncthreads();
-  block_sort_words<LW, kItems>(words, P, kLThreads, n);
+  block_sort_words<LW, kItems>(words, P, kLT, n);
   if (li < last) {
     const LeafDesc d = a.leavesSorted[li];
     const KT base = sm.glo[g];
@@ -1381,18 +1389,17 @@ __device__ __forceinline__ void leaf_words_sort(const SortArgs& a,
   }
 }
 
-// Sort up to kLThreads/P leaves of size class cls (P = 1 << cls threads each)
+// Sort up to kThreads/P leaves of size class cls (P = 1 << cls threads each)
 // from leavesSorted[first, last), results to A.  The keys are loaded once;
 // when every leaf of the CTA spans a narrow key range (the leaves of the
 // partition lie between two pivots) they are sorted as range-packed 32-bit
 // words (64-bit words for 64-bit keys with ids when that range fits), else as
 // full-range words.
-template <typename U, bool kIdx>
+template <typename U, bool kIdx, int kV>
 __device__ void sort_leaf_group(const SortArgs& a, int cls, int first, int last,
-                                typename Persist<U, kIdx>::LeafSmem& sm) {
-  using P_ = Persist<U, kIdx>;
-  using KT = typename P_::KT;
-  constexpr int kItems = Geom<U>::kLItems;
+                                typename LeafCfg<U, kIdx, kV>::Smem& sm) {
+  using KT = typename KeyCfg<U>::KT;
+  constexpr int kItems = LeafCfg<U, kIdx, kV>::kItems;
   const int P = 1 << cls;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int g = tid / P, q = tid & (P - 1);
@@ -1454,11 +1461,11 @@ __device__ void sort_leaf_group(const SortArgs& a, int cls, int first, int last,
   // 8/16-bit keys and 32-bit keys without ids already sort 32-bit words
   constexpr bool kNarrowOpt = !(sizeof(U) <= 2 || (sizeof(U) == 4 && !kIdx));
   if (kNarrowOpt && __syncthreads_and(range <= Narrow::kMaxRange)) {
-    leaf_words_sort<U, kIdx, Narrow>(a, sm, P, li, last, tmin);
+    leaf_words_sort<U, kIdx, kV, Narrow>(a, sm, P, li, last, tmin);
   } else if (sizeof(U) == 8 && kIdx && __syncthreads_and(range <= Mid::kMaxRange)) {
-    leaf_words_sort<U, kIdx, Mid>(a, sm, P, li, last, tmin);
+    leaf_words_sort<U, kIdx, kV, Mid>(a, sm, P, li, last, tmin);
   } else {
-    leaf_words_sort<U, kIdx, Full>(a, sm, P, li, last, tmin);
+    leaf_words_sort<U, kIdx, kV, Full>(a, sm, P, li, last, tmin);
   }
   __syncthreads();
 }
@@ -1480,11 +1487,12 @@ __device__ void fill_run(const SortArgs& a, const FillDesc& f) {
 // own register budget and the larger leaf CTA.
 // Launch `slice` handles the leaves of that position slice; launch 0 also
 // fills the parked pivot runs.
-template <typename U, bool kIdx>
-__global__ void __launch_bounds__(kLThreads, 2) leaf_kernel(SortArgs a, int slice) {
-  using P = Persist<U, kIdx>;
+template <typename U, bool kIdx, int kV>
+__global__ void __launch_bounds__(LeafGeom<U, kV>::kThreads, LeafGeom<U, kV>::kBlocks)
+    leaf_kernel(SortArgs a, int slice) {
+  using LC = LeafCfg<U, kIdx, kV>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  typename P::LeafSmem& sm = *reinterpret_cast<typename P::LeafSmem*>(smem_raw);
+  typename LC::Smem& sm = *reinterpret_cast<typename LC::Smem*>(smem_raw);
   Control* c = a.ctrl;
   const int tid = threadIdx.x;
   if (ld_acquire_int(&c->error) != 0) return;
@@ -1504,13 +1512,13 @@ __global__ void __launch_bounds__(kLThreads, 2) leaf_kernel(SortArgs a, int slic
     if (tid == 0) nxt = atomicAdd(wc, 1u);  // claim ahead
     if (it < leafItems) {
       // class k covers items [classItems[k], classItems[k-1])
-      int k = kLeafClasses - 1;
+      int k = LeafGeom<U, kV>::kClasses - 1;
       while (k > 0 && it >= sm.classItems[k - 1]) --k;
-      const int groups = kLThreads >> k;
+      const int groups = LC::kThreads >> k;
       const int first = sm.classOff[k] + (it - sm.classItems[k]) * groups;
       const int last = sm.classOff[k] + ld_acquire_int(&c->classCount[sb + k]);
       const int end = first + groups < last ? first + groups : last;
-      sort_leaf_group<U, kIdx>(a, k, first, end, sm);
+      sort_leaf_group<U, kIdx, kV>(a, k, first, end, sm);
     } else {
       fill_run<U, kIdx>(a, a.fills[it - leafItems]);
     }
@@ -1525,28 +1533,29 @@ __global__ void __launch_bounds__(kLThreads, 2) leaf_kernel(SortArgs a, int slic
 }
 
 // ---------------------------------------------------------------------------
-// fixed-size batched sort (MultiSort): each CTA sorts kLThreads/P arrays of
-// arrSize <= kLeafMax keys that lie back to back in memory.  Replaces the
+// fixed-size batched sort (MultiSort): each CTA sorts kThreads/P arrays of
+// arrSize <= kMax keys that lie back to back in memory.  Replaces the
 // per-thread heap sort of turtle-multi-sort.cuh:87-182.
 // ---------------------------------------------------------------------------
-template <typename U, bool kIdx>
-__global__ void __launch_bounds__(kLThreads, 2)
+template <typename U, bool kIdx, int kV>
+__global__ void __launch_bounds__(LeafGeom<U, kV>::kThreads, LeafGeom<U, kV>::kBlocks)
     multisort_kernel(U* keys, int* idx, long long numArrays, int arrSize, int cls,
                      unsigned long long flip64) {
-  using P_ = Persist<U, kIdx>;
-  using KT = typename P_::KT;
-  constexpr int kItems = Geom<U>::kLItems;
+  using LC = LeafCfg<U, kIdx, kV>;
+  using KT = typename KeyCfg<U>::KT;
+  constexpr int kItems = LC::kItems;
+  constexpr int kLT = LC::kThreads;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  typename P_::LeafSmem& sm = *reinterpret_cast<typename P_::LeafSmem*>(smem_raw);
+  typename LC::Smem& sm = *reinterpret_cast<typename LC::Smem*>(smem_raw);
   const KT flip = (KT)flip64;
   const int P = 1 << cls;
-  const int groups = kLThreads / P;
+  const int groups = kLT / P;
   const int tid = threadIdx.x;
   const long long first = (long long)blockIdx.x * groups;
   const long long na = (numArrays - first) < groups ? (numArrays - first) : groups;
   const long long base = first * arrSize;
   const int total = (int)(na * arrSize);
-  using LW = typename P_::LW;
+  using LW = typename LC::LW;
   using W = typename LW::W;
   // pad every group's tail
   {
@@ -1554,15 +1563,15 @@ __global__ void __launch_bounds__(kLThreads, 2)
     for (int j = arrSize + q; j < P * kItems; j += P) sm.words()[wpad<W>(g * P * kItems + j)] = LW::sent();
   }
   // coalesced load of the whole range
-  for (int j = tid; j < total; j += kLThreads) {
+  for (int j = tid; j < total; j += kLT) {
     const int g = j / arrSize, e = j - g * arrSize;
     const int slot = g * P * kItems + e;
     sm.words()[wpad<W>(slot)] = LW::make(kload<U, KT>(keys, base + j, flip), e);
     if (kIdx) sm.idx[slot] = idx[base + j];
   }
   __syncthreads();
-  block_sort_words<LW, kItems>(sm.words(), P, kLThreads, tid / P < na ? arrSize : 0);
-  for (int j = tid; j < total; j += kLThreads) {
+  block_sort_words<LW, kItems>(sm.words(), P, kLT, tid / P < na ? arrSize : 0);
+  for (int j = tid; j < total; j += kLT) {
     const int g = j / arrSize, e = j - g * arrSize;
     const int region = g * P * kItems;
     const W w = sm.words()[wpad<W>(region + e)];
@@ -1613,22 +1622,40 @@ static cudaError_t launch_float_order(void* keys, long long lo, long long hi, bo
 // ---------------------------------------------------------------------------
 // host-side launchers
 // ---------------------------------------------------------------------------
+// Resident CTAs per SM of each leaf geometry (set by prepare_persistent).
+static int g_leafBlocks[9][2][kLeafGeometries];
+
+template <typename U, bool kIdx, int kV>
+static cudaError_t prepare_leaf_geometry() {
+  const int lsmem = (int)leaf_smem_bytes<U, kIdx, kV>();
+  cudaError_t e = cudaFuncSetAttribute(multisort_kernel<U, kIdx, kV>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, lsmem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(leaf_kernel<U, kIdx, kV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           lsmem);
+  if (e != cudaSuccess) return e;
+  int perSM = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, leaf_kernel<U, kIdx, kV>,
+                                                    LeafGeom<U, kV>::kThreads, lsmem);
+  if (e != cudaSuccess) return e;
+  if (perSM < 1) return cudaErrorInvalidConfiguration;
+  g_leafBlocks[sizeof(U)][kIdx ? 1 : 0][kV] = perSM;
+  return cudaSuccess;
+}
+
 template <typename U, bool kIdx>
 static cudaError_t prepare_persistent(int device, int* gridOut) {
   const size_t smem = persist_smem_bytes<U, kIdx>();
-  const size_t lsmem = leaf_smem_bytes<U, kIdx>();
   cudaError_t e = cudaFuncSetAttribute(persistent_sort_kernel<U, kIdx, false>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(persistent_sort_kernel<U, kIdx, true>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(multisort_kernel<U, kIdx>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)lsmem);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(leaf_kernel<U, kIdx>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)lsmem);
-  if (e != cudaSuccess) return e;
+  if ((e = prepare_leaf_geometry<U, kIdx, 0>()) != cudaSuccess) return e;
+  if ((e = prepare_leaf_geometry<U, kIdx, 1>()) != cudaSuccess) return e;
+  if ((e = prepare_leaf_geometry<U, kIdx, 2>()) != cudaSuccess) return e;
+  if ((e = prepare_leaf_geometry<U, kIdx, 3>()) != cudaSuccess) return e;
   int perSM = 0, perSMWide = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, persistent_sort_kernel<U, kIdx, false>,
                                                     kThreads, smem);
@@ -1646,6 +1673,16 @@ static cudaError_t prepare_persistent(int device, int* gridOut) {
   return cudaSuccess;
 }
 
+template <typename U, bool kIdx, int kV>
+static cudaError_t launch_leaf(const SortArgs& a, int slice, int sms, cudaStream_t stream) {
+  const int per = g_leafBlocks[sizeof(U)][kIdx ? 1 : 0][kV];
+  leaf_kernel<U, kIdx, kV><<<(unsigned)(sms * (per > 0 ? per : 1)), LeafGeom<U, kV>::kThreads,
+                             leaf_smem_bytes<U, kIdx, kV>(), stream>>>(a, slice);
+  return cudaGetLastError();
+}
+
+// The partition kernel on `grid` CTAs (at most the resident maximum), then
+// the leaf kernel of geometry a.leafVariant once per position slice.
 template <typename U, bool kIdx>
 static cudaError_t launch_persistent(const SortArgs& a, int grid, cudaStream_t stream,
                                      cudaEvent_t mid, const cudaEvent_t* sliceDone) {
@@ -1672,10 +1709,15 @@ static cudaError_t launch_persistent(const SortArgs& a, int grid, cudaStream_t s
   int sms = 0, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (sms < 1) sms = 1;
   for (int sl = 0; sl < a.slices; ++sl) {
-    leaf_kernel<U, kIdx><<<(unsigned)(sms > 0 ? 2 * sms : 2), kLThreads,
-                           leaf_smem_bytes<U, kIdx>(), stream>>>(a, sl);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    switch (a.leafVariant) {
+      case 0: e = launch_leaf<U, kIdx, 0>(a, sl, sms, stream); break;
+      case 2: e = launch_leaf<U, kIdx, 2>(a, sl, sms, stream); break;
+      case 3: e = launch_leaf<U, kIdx, 3>(a, sl, sms, stream); break;
+      default: e = launch_leaf<U, kIdx, 1>(a, sl, sms, stream); break;
+    }
+    if (e != cudaSuccess) return e;
     if (kFloatable && a.fbits != 0) {
       // keys of this slice are final: back from totalOrder images
       const long long lo = (sl * a.n + a.slices - 1) / a.slices;
@@ -1689,24 +1731,38 @@ static cudaError_t launch_persistent(const SortArgs& a, int grid, cudaStream_t s
   return cudaSuccess;
 }
 
-template <typename U, bool kIdx>
-static cudaError_t launch_multisort(void* keys, int* idx, long long numArrays, int arrSize,
-                                    unsigned long long flip, int fbits, cudaStream_t stream) {
-  constexpr int kItems = Geom<U>::kLItems;
+template <typename U, bool kIdx, int kV>
+static cudaError_t launch_multisort_geom(void* keys, int* idx, long long numArrays, int arrSize,
+                                         unsigned long long flip, cudaStream_t stream) {
+  constexpr int kItems = LeafGeom<U, kV>::kItems, kLT = LeafGeom<U, kV>::kThreads;
   int cls = 0;
   while ((1 << cls) * kItems < arrSize) ++cls;
-  const int groups = kLThreads >> cls;
+  const int groups = kLT >> cls;
   const long long blocks = (numArrays + groups - 1) / groups;
   if (blocks <= 0) return cudaSuccess;
+  multisort_kernel<U, kIdx, kV><<<(unsigned)blocks, kLT, leaf_smem_bytes<U, kIdx, kV>(), stream>>>(
+      (U*)keys, idx, numArrays, arrSize, cls, flip);
+  return cudaGetLastError();
+}
+
+template <typename U, bool kIdx>
+static cudaError_t launch_multisort(void* keys, int* idx, long long numArrays, int arrSize,
+                                    unsigned long long flip, int fbits, int geometry,
+                                    cudaStream_t stream) {
+  if (numArrays <= 0) return cudaSuccess;
   constexpr bool kFloatable = sizeof(U) >= 4;
   const long long total = numArrays * (long long)arrSize;
   cudaError_t e;
   if (kFloatable && fbits != 0 &&
       (e = launch_float_order<U>(keys, 0, total, false, nullptr, stream)) != cudaSuccess)
     return e;
-  multisort_kernel<U, kIdx><<<(unsigned)blocks, kLThreads, leaf_smem_bytes<U, kIdx>(), stream>>>(
-      (U*)keys, idx, numArrays, arrSize, cls, flip);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  switch (geometry) {
+    case 0: e = launch_multisort_geom<U, kIdx, 0>(keys, idx, numArrays, arrSize, flip, stream); break;
+    case 2: e = launch_multisort_geom<U, kIdx, 2>(keys, idx, numArrays, arrSize, flip, stream); break;
+    case 3: e = launch_multisort_geom<U, kIdx, 3>(keys, idx, numArrays, arrSize, flip, stream); break;
+    default: e = launch_multisort_geom<U, kIdx, 1>(keys, idx, numArrays, arrSize, flip, stream); break;
+  }
+  if (e != cudaSuccess) return e;
   if (kFloatable && fbits != 0) return launch_float_order<U>(keys, 0, total, true, nullptr, stream);
   return cudaSuccess;
 }
@@ -1738,9 +1794,9 @@ cudaError_t kernels_launch_persistent(int width, bool hasIdx, const SortArgs& a,
 
 cudaError_t kernels_launch_multisort(int width, bool hasIdx, void* keys, int* idx,
                                      long long numArrays, int arrSize, unsigned long long flip,
-                                     int fbits, cudaStream_t stream) {
+                                     int fbits, int geometry, cudaStream_t stream) {
   TURTLE_WIDTH_DISPATCH(width, hasIdx, (launch_multisort<U, I>(keys, idx, numArrays, arrSize, flip,
-                                                               fbits, stream)));
+                                                               fbits, geometry, stream)));
 }
 
 int kernels_tile_elems(int width) {
@@ -1753,14 +1809,27 @@ int kernels_tile_elems(int width) {
   }
 }
 
-int kernels_leaf_max(int width) {
-  switch (width) {
-    case 1: return Geom<uint8_t>::kLeafMax;
-    case 2: return Geom<uint16_t>::kLeafMax;
-    case 4: return Geom<uint32_t>::kLeafMax;
-    case 8: return Geom<uint64_t>::kLeafMax;
-    default: return 0;
+// Geometry of leaf / MultiSort variant g for keys of `width` bytes: CTA
+// threads, keys per thread, capacity, size classes.
+void kernels_leaf_geometry(int width, int g, int* threads, int* items, int* capacity,
+                           int* classes) {
+  const int base = width == 8 ? 8 : 16;
+  const int t = g == 0 ? 256 : g == 2 ? 1024 : 512;
+  const int it = g == 3 ? base / 2 : base;
+  if (threads) *threads = t;
+  if (items) *items = it;
+  if (capacity) *capacity = t * it;
+  if (classes) {
+    int c = 1;
+    while ((1 << (c - 1)) < t) ++c;
+    *classes = c;
   }
+}
+
+int kernels_leaf_max(int width) {
+  int cap = 0;
+  kernels_leaf_geometry(width, kDefaultLeafGeometry, nullptr, nullptr, &cap, nullptr);
+  return (width == 1 || width == 2 || width == 4 || width == 8) ? cap : 0;
 }
 
 }  // namespace turtle

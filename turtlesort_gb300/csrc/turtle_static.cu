@@ -115,8 +115,10 @@ extern "C" turtle_status turtle_sort_device_noalloc(turtle_dtype dtype, void* d_
   const Plan p = plan_for(width);
   const bool hasIdx = d_idx != nullptr;
   cudaStream_t cs = (cudaStream_t)stream;
+  // the compile-time defaults: the scratch array is laid out for them
   turtle::SortArgs a = turtle::bind_args(d_keys, d_idx, st->base, (int*)(st->base + p.offIdx),
-                                         st->base + p.offWs, p.lay, nullptr, 0, n, dtype);
+                                         st->base + p.offWs, p.lay, nullptr, 0, n, dtype,
+                                         turtle::kRuleAuto, turtle::tune_defaults(width, n));
   // the previous call's work-list header must not leak into this one
   if ((e = cudaMemsetAsync(a.ctrl, 0, sizeof(turtle::Control), cs)) != cudaSuccess)
     return cuda_status(e);

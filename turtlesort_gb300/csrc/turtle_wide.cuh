@@ -131,8 +131,9 @@ __device__ __forceinline__ void count31_tile_warp(const SortArgs& a, int pass, i
                                                   unsigned& phases, int& accSeg, int& accCnt) {
   using P = Persist<U, kIdx>;
   using KT = typename P::KT;
-  constexpr int kItems = P::kItems, kWCH = P::kWCH, kShift = P::kTileShift;
-  static_assert(P::kTile / 32 < 256, "per-lane tile counts are 8-bit");
+  constexpr int kItems = P::kItems, kWCH = P::kWCH;
+  // tiles are at most 4096 keys: a lane tallies at most 128 keys of a tile
+  const int kShift = a.tileShift;
   const int par = pass & 1;
   const int lane = threadIdx.x & 31;
   const U* src = (const U*)(par ? a.keysB : a.keysA);
@@ -150,8 +151,8 @@ __device__ __forceinline__ void count31_tile_warp(const SortArgs& a, int pass, i
     ws.t.pivSeg = td.seg;
   }
   const KT* q = ws.t.q;
-  // per-lane class tallies, one byte each (a lane sees at most kTile / 32 =
-  // 64 keys of a tile): cnt[32 * k + lane], in the stage buffer, which COUNT
+  // per-lane class tallies, one byte each (a lane sees at most tile / 32 <=
+  // 128 keys of a tile): cnt[32 * k + lane], in the stage buffer, which COUNT
   // does not use otherwise
   static_assert(sizeof(ws.sk) >= 32 * 32, "the stage holds 32 x 32 byte tallies");
   unsigned char* cnt = reinterpret_cast<unsigned char*>(ws.sk);
@@ -235,8 +236,7 @@ __device__ __noinline__ void plan31_item(const SortArgs& a, int pass, int item,
                                          typename Persist<U, kIdx>::Smem& sm) {
   using P = Persist<U, kIdx>;
   using KT = typename P::KT;
-  constexpr int kTile = P::kTile, kLeafMax = P::kLeafMax;
-  static_assert(kLeafMax >= kWideSamples, "segments hold at least kWideSamples keys");
+  const int kLeafMax = a.leafCut;  // at least kWideSamples: every segment holds its samples
   const int par = pass & 1;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int seg = __ldcg(&a.planSeg[par][item]);
@@ -347,7 +347,7 @@ __device__ __noinline__ void plan31_item(const SortArgs& a, int pass, int item,
             push_leaf(a, pos, m, dstIsA ? 0 : 1);
           } else {
             int tb = 0, ntc = 0;
-            si = alloc_segment<kTile>(a, nextPar, pos, m, &tb, &ntc, true);
+            si = alloc_segment(a, nextPar, pos, m, &tb, &ntc, true);
             if (si >= 0) a.segs[nextPar][si].nsamp = kWideSamples;
             sm.gTb[g] = tb;
             sm.gNt[g] = si >= 0 ? ntc : 0;
@@ -368,7 +368,7 @@ __device__ __noinline__ void plan31_item(const SortArgs& a, int pass, int item,
   if (tid < 16) sdp->childSeg[tid] = sm.gSeg[tid];
   for (int g = 0; g < 16; ++g) {
     if (sm.gSeg[g] >= 0)
-      write_tiles<kTile>(a, nextPar, sm.gSeg[g], sm.gTb[g], sm.gNt[g], sm.gStart[g], sm.gN[g],
+      write_tiles(a, nextPar, sm.gSeg[g], sm.gTb[g], sm.gNt[g], sm.gStart[g], sm.gN[g],
                          tid, kThreads);
   }
   __syncthreads();
@@ -384,7 +384,7 @@ __device__ __noinline__ void plan31_small_warp(const SortArgs& a, int pass, int 
                                                WidePivots<typename Persist<U, kIdx>::KT>* scratch) {
   using P = Persist<U, kIdx>;
   using KT = typename P::KT;
-  constexpr int kTile = P::kTile, kLeafMax = P::kLeafMax;
+  const int kLeafMax = a.leafCut;
   const int par = pass & 1;
   const int lane = threadIdx.x & 31;
   SegDesc* sdp = &a.segs[par][seg];
@@ -443,7 +443,7 @@ __device__ __noinline__ void plan31_small_warp(const SortArgs& a, int pass, int 
       if (m <= kLeafMax) {
         push_leaf(a, pos, m, dstIsA ? 0 : 1);
       } else {
-        si = alloc_segment<kTile>(a, nextPar, pos, m, &tb, &ntc, true);
+        si = alloc_segment(a, nextPar, pos, m, &tb, &ntc, true);
         if (si >= 0) a.segs[nextPar][si].nsamp = kWideSamples;
       }
     }
@@ -464,7 +464,7 @@ __device__ __noinline__ void plan31_small_warp(const SortArgs& a, int pass, int 
       const int cnt2 = __shfl_sync(kFull, ntc, src);
       const long long cs = __shfl_sync(kFull, pos, src);
       const long long cn = __shfl_sync(kFull, m, src);
-      write_tiles<kTile>(a, nextPar, s, ctb, cnt2, cs, cn, lane, 32);
+      write_tiles(a, nextPar, s, ctb, cnt2, cs, cn, lane, 32);
     }
   }
   if (lane < 16) sdp->childSeg[lane] = gseg;
@@ -500,7 +500,8 @@ __device__ __forceinline__ void scatter31_tile_warp(const SortArgs& a, int pass,
                                                     unsigned& phases) {
   using P = Persist<U, kIdx>;
   using KT = typename P::KT;
-  constexpr int kItems = P::kItems, kWCH = P::kWCH, kShift = P::kTileShift;
+  constexpr int kItems = P::kItems, kWCH = P::kWCH;
+  const int kShift = a.tileShift;
   const int par = pass & 1;
   const KT flip = (KT)a.flip;
   const int lane = threadIdx.x & 31;
