@@ -377,9 +377,14 @@ def main() -> None:
                     choices=["sort64m", "plain12m", "sweep", "multisort", "batched", "wide",
                              "floats", "serving"],
                     help="sort64m (default) is the headline line; the others print their own")
-    ap.add_argument("--requests", type=int, default=1000, help="serving: requests in the sample")
+    ap.add_argument("--requests", type=int, default=20000, help="serving: requests in the stream")
     ap.add_argument("--rate", type=float, default=0.0,
-                    help="serving: arrivals per second (0: 1.5x the serial StartSorting rate)")
+                    help="serving: Poisson arrivals per second (0: 60%% of the closed-loop rate)")
+    ap.add_argument("--outstanding", type=int, default=64,
+                    help="serving: requests in flight in the closed-loop run")
+    ap.add_argument("--arena-gb", type=int, default=8, help="serving: pinned host arena (GiB)")
+    ap.add_argument("--serial-sample", type=int, default=1000,
+                    help="serving: requests in the serial StartSorting baseline")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3

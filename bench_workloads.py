@@ -280,15 +280,102 @@ def batched(args):
                "speedup_vs_per_array": (num / e2e) * per_array})
 
 
+class _Arena:
+    """First-fit allocator over one pinned host buffer (16-byte blocks)."""
+
+    def __init__(self, torch, nbytes):
+        self.t = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+        self.a = self.t.numpy()
+        self.free = [(0, nbytes)]
+        self.cv = threading.Condition()
+
+    def try_alloc(self, nbytes):
+        """(offset, size) of a free block, or None when nothing fits."""
+        nbytes = (nbytes + 15) // 16 * 16
+        with self.cv:
+            for j, (o, sz) in enumerate(self.free):
+                if sz >= nbytes:
+                    self.free[j] = (o + nbytes, sz - nbytes)
+                    if self.free[j][1] == 0:
+                        self.free.pop(j)
+                    return o, nbytes
+            return None
+
+    def alloc(self, nbytes):
+        while True:
+            blk = self.try_alloc(nbytes)
+            if blk is not None:
+                return blk
+            self.wait_release()
+
+    def wait_release(self, timeout=0.05):
+        with self.cv:
+            self.cv.wait(timeout)
+
+    def release(self, o, nbytes):
+        with self.cv:
+            self.free.append((o, nbytes))
+            self.free.sort()
+            merged = []
+            for fo, fs in self.free:
+                if merged and merged[-1][0] + merged[-1][1] == fo:
+                    merged[-1] = (merged[-1][0], merged[-1][1] + fs)
+                else:
+                    merged.append((fo, fs))
+            self.free = merged
+            self.cv.notify_all()
+
+
+_MIX1 = np.uint64(0xBF58476D1CE4E5B9)
+_MIX2 = np.uint64(0x94D049BB133111EB)
+
+
+def _multiset_sum(k: np.ndarray) -> int:
+    """Order-independent checksum of the keys' bit patterns (splitmix64
+    finaliser of each, summed mod 2^64)."""
+    x = k.view(np.uint16 if k.itemsize == 2 else np.uint32 if k.itemsize == 4 else np.uint64)
+    x = x.astype(np.uint64)
+    with np.errstate(over="ignore"):
+        x = (x ^ (x >> np.uint64(30))) * _MIX1
+        x = (x ^ (x >> np.uint64(27))) * _MIX2
+        x = x ^ (x >> np.uint64(31))
+        return int(np.sum(x, dtype=np.uint64))
+
+
+def _check_request(keys_in, out_k, out_i):
+    """Exact check of one served request: keys sorted and the same multiset;
+    with ids (positions), the ids are a permutation that reorders the input
+    to the output with equal keys in input order (that is the stable sort)."""
+    n = keys_in.size
+    if n > 1 and not np.all(out_k[1:] >= out_k[:-1]):
+        return "keys not sorted"
+    if out_i is None:
+        return None if _multiset_sum(keys_in) == _multiset_sum(out_k) else "keys changed"
+    if n and (out_i.min() < 0 or out_i.max() >= n or np.bincount(out_i, minlength=n).max() != 1):
+        return "ids are not a permutation"
+    if not np.array_equal(keys_in[out_i], out_k):
+        return "ids do not reorder the keys"
+    same = out_k[1:] == out_k[:-1]
+    if n > 1 and not np.all(out_i[1:][same] > out_i[:-1][same]):
+        return "equal keys out of input order"
+    return None
+
+
 def serving(args):
-    """A bounded sample of the serving stream: args.requests requests with
-    log-uniform sizes in [1024, 16 * 2^20], dtype int32 60% / int64 25% /
-    uint16 15%, half with ids, HBM budget 64 GB.  Three runs over the same
-    pre-filled pinned buffers (refilled, untimed, before each run):
-      serial      one StartSorting + Sync per request, back to back;
-      saturated   every request submitted at once to the server (throughput);
-      poisson     Poisson arrivals at half the saturated request rate
-                  (latency from arrival to completion: p50 / p99)."""
+    """The serving stream of the benchmark suite: args.requests requests
+    (20,000 by default) with log-uniform sizes in [1024, 16 * 2^20], dtype
+    int32 60% / int64 25% / uint16 15%, half with an int32 index (= position),
+    values uniform over each dtype's range (slices of a seeded random pool),
+    HBM budget 64 GB.  Host buffers come from a pinned arena (requests wait
+    for room, as a server's callers would); every result is checked exactly
+    on a thread pool (_check_request).  Runs:
+      closed loop  up to --outstanding requests in flight (throughput);
+      poisson      Poisson arrivals at --rate (default: 60% of the closed-loop
+                   request rate), latency from arrival to completion;
+      serial       one StartSorting + Sync per request for the first
+                   --serial-sample requests (the reference's way to serve)."""
+    import concurrent.futures as cf
+    import os
     torch = _torch()
     nreq = args.requests
     rng_u = dg.uniform_real(4 * nreq, dg.seed_for(4))
@@ -296,113 +383,173 @@ def serving(args):
     dts = np.where(rng_u[nreq:2 * nreq] < 0.60, 0, np.where(rng_u[nreq:2 * nreq] < 0.85, 1, 2))
     with_idx = rng_u[2 * nreq:3 * nreq] < 0.5
     dtypes = [np.int32, np.int64, np.uint16]
-    pool = dg.uniform(np.uint64, 1 << 25, dg.seed_for(4) + 1)  # 256 MiB of random words
+    pool = dg.uniform(np.uint64, 1 << 26, dg.seed_for(4) + 1)  # 512 MiB of random words
     keys_total = int(sizes.sum())
-    kb = [int(sizes[r]) * np.dtype(dtypes[dts[r]]).itemsize for r in range(nreq)]
-    ib = [int(sizes[r]) * 4 if with_idx[r] else 0 for r in range(nreq)]
-    koff = np.concatenate([[0], np.cumsum([(x + 15) // 16 * 16 for x in kb])])
-    ioff = np.concatenate([[0], np.cumsum([(x + 15) // 16 * 16 for x in ib])])
-    arena_k = torch.empty(int(koff[-1]), dtype=torch.uint8, pin_memory=True)
-    arena_i = torch.empty(max(int(ioff[-1]), 16), dtype=torch.uint8, pin_memory=True)
-    ak, ai = arena_k.numpy(), arena_i.numpy()
-    views = []
-    for r in range(nreq):
+    arena = _Arena(torch, args.arena_gb << 30)
+    checker = cf.ThreadPoolExecutor(max(2, (os.cpu_count() or 4) - 2))
+
+    def request_input(r):
         dt = np.dtype(dtypes[dts[r]])
         n = int(sizes[r])
-        kv = ak[koff[r]: koff[r] + kb[r]].view(dt)
-        iv = ai[ioff[r]: ioff[r] + ib[r]].view(np.int32) if with_idx[r] else None
-        views.append((kv, iv))
+        words = (n * dt.itemsize + 7) // 8
+        off = int((r * 7919 * 7919) % (pool.size - words))
+        return pool[off: off + words].view(dt)[:n]
 
-    def refill():
-        for r, (kv, iv) in enumerate(views):
-            words = (kv.nbytes + 7) // 8
-            off = int((r * 7919) % (pool.size - words))
-            kv[:] = pool[off: off + words].view(kv.dtype)[: kv.size]
-            if iv is not None:
-                iv[:] = np.arange(iv.size, dtype=np.int32)
+    def need(r):
+        n = int(sizes[r])
+        return n * np.dtype(dtypes[dts[r]]).itemsize + 16 + (4 * n if with_idx[r] else 0)
 
-    def check():
-        for r, (kv, iv) in enumerate(views):
-            if kv.size > 1 and not np.all(kv[:-1] <= kv[1:]):
-                raise RuntimeError(f"request {r} not sorted")
+    def stage(r, blk=None):
+        """Pinned key / id buffers of request r, filled with its input."""
+        dt = np.dtype(dtypes[dts[r]])
+        n = int(sizes[r])
+        kb = n * dt.itemsize
+        ib = 4 * n if with_idx[r] else 0
+        o, sz = blk if blk is not None else arena.alloc(kb + 16 + ib)
+        kv = arena.a[o: o + kb].view(dt)
+        kv[:] = request_input(r)
+        iv = None
+        if ib:
+            io = o + (kb + 15) // 16 * 16
+            iv = arena.a[io: io + ib].view(np.int32)
+            iv[:] = np.arange(n, dtype=np.int32)
+        return kv, iv, (o, sz)
 
-    # serial baseline
-    refill()
-    sorters = {}
-    t_serial = 0.0
-    for r, (kv, iv) in enumerate(views):
-        key = (int(dts[r]), iv is not None)
-        if key not in sorters:
-            sorters[key] = ts.TurtleSort(dtypes[dts[r]], int(sizes.max()), track_index=key[1])
-        t0 = time.perf_counter()
-        sorters[key].StartSorting(kv, iv)
-        sorters[key].Sync()
-        t_serial += time.perf_counter() - t0
-    for s in sorters.values():
-        s.close()
-    check()
-    serial_kps = keys_total / t_serial
+    failures = []
+
+    def verify(r, kv, iv, blk):
+        err = _check_request(request_input(r), kv, iv)
+        if err:
+            failures.append((r, err))
+        arena.release(*blk)
 
     srv = ts.TurtleServer(hbm_budget_bytes=64 << 30)
-    # warm the server's pool and kernels with one pass, untimed
-    refill()
-    for t in [srv.submit(kv, iv) for kv, iv in views[: min(8, nreq)]]:
-        srv.wait(t)
-    # saturated: everything submitted at once
-    refill()
-    t0 = time.perf_counter()
-    tickets = [srv.submit(kv, iv) for kv, iv in views]
-    for t in tickets:
-        srv.wait(t)
-    t_sat = time.perf_counter() - t0
-    check()
+    # warm-up (kernels, pool), untimed
+    for r in range(min(8, nreq)):
+        kv, iv, blk = stage(r)
+        srv.wait(srv.submit(kv, iv))
+        arena.release(*blk)
+
+    def closed_loop(limit):
+        inflight = []
+        lat = []
+        checks = []
+        t0 = time.perf_counter()
+        def retire():
+            rr, tk, k2, i2, b2 = inflight.pop(0)
+            lat.append(srv.wait(tk))
+            checks.append(checker.submit(verify, rr, k2, i2, b2))
+
+        for r in range(nreq):
+            blk = arena.try_alloc(need(r))
+            while blk is None:  # the arena is full: retire the oldest, or wait for a check
+                if inflight:
+                    retire()
+                else:
+                    arena.wait_release()
+                blk = arena.try_alloc(need(r))
+            kv, iv, blk = stage(r, blk)
+            inflight.append((r, srv.submit(kv, iv), kv, iv, blk))
+            while len(inflight) >= limit:
+                retire()
+        for rr, tk, k2, i2, b2 in inflight:
+            lat.append(srv.wait(tk))
+            checks.append(checker.submit(verify, rr, k2, i2, b2))
+        t = time.perf_counter() - t0
+        for c in checks:
+            c.result()
+        return t, lat
+
+    st0 = srv.stats()
+    t_sat, _ = closed_loop(args.outstanding)
+    st1 = srv.stats()
     sat_kps = keys_total / t_sat
-    # Poisson arrivals at half the saturated request rate
-    rate = args.rate if args.rate > 0 else 0.5 * nreq / t_sat
+    sat_rps = nreq / t_sat
+    # Poisson arrivals
+    rate = args.rate if args.rate > 0 else 0.6 * sat_rps
     gaps = -np.log(np.maximum(rng_u[3 * nreq:4 * nreq], 1e-12)) / rate
     arrivals = np.cumsum(gaps)
-    refill()
     lat = [0.0] * nreq
-    done_q = []
+    pending = []
     cv = threading.Condition()
+    done_flag = [False]
 
     def waiter():
-        for r in range(nreq):
+        while True:
             with cv:
-                while len(done_q) <= r:
+                while not pending and not done_flag[0]:
                     cv.wait()
-                ticket, t_arr = done_q[r]
-            srv.wait(ticket)
+                if not pending and done_flag[0]:
+                    return
+                r, tk, t_arr, kv, iv, blk = pending.pop(0)
+            srv.wait(tk)
             lat[r] = time.perf_counter() - t_arr
+            checker.submit(verify, r, kv, iv, blk)
 
     th = threading.Thread(target=waiter)
     th.start()
     t_start = time.perf_counter()
-    for r, (kv, iv) in enumerate(views):
+    for r in range(nreq):
         target = t_start + arrivals[r]
         now = time.perf_counter()
         if target > now:
             time.sleep(target - now)
-        ticket = srv.submit(kv, iv)
+        kv, iv, blk = stage(r)
+        tk = srv.submit(kv, iv)
         with cv:
-            done_q.append((ticket, max(target, t_start)))
+            pending.append((r, tk, max(target, t_start), kv, iv, blk))
             cv.notify_all()
+    with cv:
+        done_flag[0] = True
+        cv.notify_all()
     th.join()
     t_pois = time.perf_counter() - t_start
-    check()
-    st = srv.stats()
+    st2 = srv.stats()
     srv.close()
+    checker.shutdown(wait=True)
+    # serial StartSorting + Sync on a sample
+    ns = min(args.serial_sample, nreq)
+    sorters = {}
+    t_serial = 0.0
+    serial_keys = 0
+    for r in range(ns):
+        key = (int(dts[r]), bool(with_idx[r]))
+        if key not in sorters:
+            sorters[key] = ts.TurtleSort(dtypes[dts[r]], 16 << 20, track_index=key[1])
+        kv, iv, blk = stage(r)
+        t0 = time.perf_counter()
+        sorters[key].StartSorting(kv, iv)
+        sorters[key].Sync()
+        t_serial += time.perf_counter() - t0
+        serial_keys += kv.size
+        err = _check_request(request_input(r), kv, iv)
+        if err:
+            failures.append((r, "serial: " + err))
+        arena.release(*blk)
+    for srt in sorters.values():
+        srt.close()
+    if failures:
+        raise RuntimeError(f"{len(failures)} requests wrong, first: {failures[:3]}")
+    serial_kps = serial_keys / t_serial
     lat_ms = np.array(lat) * 1e3
-    _line("served keys/s (request stream, continuous batching, saturated)", sat_kps, "keys/s", args,
-          {"workload": f"{nreq} requests (bounded sample of 20,000), sizes log-uniform "
-                       f"[1024, 16*2^20], int32 60%/int64 25%/uint16 15%, half with ids, "
-                       f"HBM budget 64 GB", "requests": nreq, "keys": keys_total},
-          {"dtype": "mixed",
+    batches_sat = st1["batches"] - st0["batches"]
+    batches_pois = st2["batches"] - st1["batches"]
+    _line("served keys/s (request stream, continuous batching, closed loop)", sat_kps, "keys/s",
+          args,
+          {"workload": f"{nreq} requests, sizes log-uniform [1024, 16*2^20], int32 60%/int64 "
+                       f"25%/uint16 15%, half with int32 ids, HBM budget 64 GB",
+           "requests": nreq, "keys": keys_total, "outstanding": args.outstanding},
+          {"dtype": "mixed", "requests_per_s": sat_rps, "batches": batches_sat,
+           "requests_per_batch": nreq / max(batches_sat, 1),
            "poisson": {"arrival_rate_per_s": rate, "p50_ms": float(np.percentile(lat_ms, 50)),
                        "p99_ms": float(np.percentile(lat_ms, 99)),
-                       "keys_per_s": keys_total / t_pois},
-           "batches_total": st["batches"], "serial_startsorting_keys_per_s": serial_kps,
+                       "mean_ms": float(lat_ms.mean()), "keys_per_s": keys_total / t_pois,
+                       "batches": batches_pois,
+                       "requests_per_batch": nreq / max(batches_pois, 1)},
+           "serial_startsorting_keys_per_s": serial_kps,
+           "serial_sample": f"first {ns} requests, one StartSorting + Sync each",
            "speedup_vs_serial": sat_kps / serial_kps,
+           "checked": f"all {nreq} requests of both runs and the serial sample, exactly",
            "e2e": {"value": sat_kps, "unit": "keys/s",
                    "note": "pinned host buffers; host<->device copies inside every request"}})
 

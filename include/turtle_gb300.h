@@ -158,11 +158,12 @@ int64_t turtle_noalloc_max_elements(void);
  * (turtle-sort.cuh:124-258); a serving process calls it once per request,
  * serially.  A turtle_server takes requests of any of the eight dtypes, with
  * or without ids, from any host thread.  A scheduler thread admits waiting
- * requests in arrival order while their device memory fits the HBM budget,
- * fuses consecutive requests of the same (dtype, ids) group into one batched
- * persistent launch, and keeps up to three batches in flight (copy in, sort,
- * copy out overlap on separate streams).  Results are identical to sorting
- * each request alone. */
+ * requests while their device memory fits the HBM budget: the oldest waiting
+ * request opens a batch and the requests of its (dtype, ids) group among the
+ * next 256 waiting ones join it, in one batched persistent launch.  Up to
+ * four batches are in flight: copies in and out overlap other batches'
+ * sorts, and two batches sort at once, each on half of the GPU.  Results are
+ * identical to sorting each request alone. */
 typedef struct turtle_server turtle_server; /* opaque */
 
 typedef struct turtle_server_stats {

@@ -97,3 +97,46 @@ def test_multisort_every_geometry(gpu, dtype, arr):
         exp_i = (order + (np.arange(num) * arr)[:, None]).astype(np.int32).reshape(-1)
         assert np.array_equal(d.cpu().numpy(), exp_k), f"geometry {g}"
         assert np.array_equal(ids.cpu().numpy(), exp_i), f"geometry {g}"
+
+
+@pytest.mark.parametrize("dtype", [np.int32, np.int16, np.uint8, np.int64, np.float32])
+def test_largest_leaves_with_ids(gpu, dtype):
+    """Arrays that fill the largest shared-memory geometry are sorted as one
+    leaf: positions up to the geometry's capacity must survive the packing of
+    narrow-range keys (and of full-range keys)."""
+    cap = ts.leaf_geometry(dtype, 2)["capacity"]
+    with TurtleSort(dtype, cap, track_index=True) as s:
+        s.set_config("two_level", 11, 2, cap, 1)
+        for n in (cap, cap - 1, cap // 2 + 1, 1000):
+            for span in (7, 1000, None):
+                if np.dtype(dtype).kind == "f":
+                    keys = (dg.uniform(np.int32, n, n + 3, 0, span or 2**30)
+                            .astype(np.float64) * 0.25).astype(dtype)
+                else:
+                    keys = (dg.uniform(dtype, n, n + 3, 0, span) if span
+                            else dg.uniform(dtype, n, n + 3))
+                idx = np.arange(n, dtype=np.int32)
+                k, i = keys.copy(), idx.copy()
+                s.StartSorting(k, i)
+                s.Sync()
+                ek, ei = _stable(keys, idx)
+                assert np.array_equal(k, ek), (n, span)
+                assert np.array_equal(i, ei), (n, span)
+
+
+@pytest.mark.parametrize("form", ["sampled", "two_level"])
+def test_big_leaves_at_scale(gpu, form):
+    """The configuration that first exposed the position-width limit: 2^24
+    keys, 1024-key tiles, the 1024-thread geometry with 16384-key leaves."""
+    n = 1 << 24
+    keys = dg.uniform(np.int32, n, 4711)
+    idx = np.arange(n, dtype=np.int32)
+    with TurtleSort(np.int32, n, track_index=True) as s:
+        s.set_config(form, 10, 2, ts.leaf_geometry(np.int32, 2)["capacity"], 1)
+        k, i = keys.copy(), idx.copy()
+        s.StartSorting(k, i)
+        s.Sync()
+    assert np.all(k[1:] >= k[:-1])
+    assert np.array_equal(keys[i], k)
+    same = k[1:] == k[:-1]
+    assert np.all(i[1:][same] > i[:-1][same])

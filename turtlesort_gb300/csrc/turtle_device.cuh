@@ -549,22 +549,25 @@ struct LeafWord<uint64_t, true> {
 
 // Range-packed words for arrays whose keys span a narrow range (the leaves of
 // the partition lie between two pivots): the key minus the array's smallest
-// key, shifted above a 13-bit position when there are ids (positions are
-// below kLeafMax <= 8192).  Usable when max - min <= kMaxRange, which keeps
-// every real word below the padding word.  Narrower words halve the ALU work
-// of every compare and select in the network and the merges.
+// key, shifted above a `sh`-bit position when there are ids (sh = log2 of
+// the group's slot count, so every position fits).  Usable when
+// max - min <= max_range(sh), which keeps every real word below the padding
+// word.  Narrower words halve the ALU work of every compare and select in the
+// network and the merges.
 template <typename KT, typename Wt, bool kIdx>
 struct RangeWord {
   using W = Wt;
-  static constexpr int kPosBits = kIdx ? 13 : 0;
-  static constexpr unsigned long long kMaxRange =
-      (unsigned long long)(W(~W(0)) >> kPosBits) - (kIdx ? 1ull : 0ull);
-  __device__ __forceinline__ static W make(KT k, KT lo, int pos) {
-    return (W(k - lo) << kPosBits) | W(kIdx ? (unsigned)pos : 0u);
+  __host__ __device__ static constexpr unsigned long long max_range(int sh) {
+    return (unsigned long long)(W(~W(0)) >> (kIdx ? sh : 0)) - (kIdx ? 1ull : 0ull);
   }
-  __device__ __forceinline__ static KT key(W w, KT lo) { return lo + KT(w >> kPosBits); }
-  __device__ __forceinline__ static int pos(W w) {
-    return (int)(w & W((1ull << kPosBits) - 1ull));
+  __device__ __forceinline__ static W make(KT k, KT lo, int pos, int sh) {
+    return kIdx ? (W(k - lo) << sh) | W((unsigned)pos) : W(k - lo);
+  }
+  __device__ __forceinline__ static KT key(W w, KT lo, int sh) {
+    return lo + KT(kIdx ? w >> sh : w);
+  }
+  __device__ __forceinline__ static int pos(W w, int sh) {
+    return kIdx ? (int)(w & W((1ull << sh) - 1ull)) : 0;
   }
   __device__ __forceinline__ static bool less(W a, W b) { return a < b; }
   __device__ __forceinline__ static W sent() { return W(~W(0)); }
@@ -576,10 +579,10 @@ struct FullWord : LeafWord<U, kIdx> {
   using Base = LeafWord<U, kIdx>;
   using W = typename Base::W;
   template <typename KT>
-  __device__ __forceinline__ static W make(KT k, KT, int pos) { return Base::make(k, pos); }
+  __device__ __forceinline__ static W make(KT k, KT, int pos, int) { return Base::make(k, pos); }
   template <typename KT>
-  __device__ __forceinline__ static KT key(W w, KT) { return (KT)Base::key(w); }
-  static constexpr unsigned long long kMaxRange = ~0ull;
+  __device__ __forceinline__ static KT key(W w, KT, int) { return (KT)Base::key(w); }
+  __device__ __forceinline__ static int pos(W w, int) { return Base::pos(w); }
 };
 
 // Bank-conflict padding for word arrays: one spare slot per 128 bytes, so a

@@ -5,17 +5,21 @@
 // sizes and dtypes arrive at any time from any host thread.  A scheduler
 // thread
 //   * retires finished batches (their device memory returns to the budget);
-//   * admits waiting requests in arrival order while the HBM budget allows,
-//     fusing consecutive requests of the same (dtype, ids) group into one
-//     batched persistent launch (arrays packed back to back with an offsets
-//     array, exactly the turtle_sort_batched_device form);
-//   * keeps up to kSlots batches in flight as a three-stage pipeline on three
-//     streams (copy in, sort, copy out), so one batch's copies overlap another
-//     batch's sort.  Requests that arrive while batches are on the GPU join the
-//     next batch as memory frees up.
-// Sort kernels of different batches run one after another on the sort
-// stream (each is a cooperative launch sized to the whole GPU); the copies of
-// the neighbouring batches run beside them.
+//   * admits waiting requests while the HBM budget allows: the oldest waiting
+//     request opens a batch, and every request of its (dtype, ids) group
+//     within the first kWindow waiting requests joins it (in arrival order),
+//     up to the batch limits -- one batched persistent launch with the arrays
+//     packed back to back and an offsets array, exactly the
+//     turtle_sort_batched_device form; requests of other groups keep their
+//     place in the queue;
+//   * keeps up to kSlots batches in flight as a pipeline of copy-in, sort and
+//     copy-out streams, so one batch's copies overlap other batches' sorts.
+//     Requests that arrive while batches are on the GPU join the next batch as
+//     memory frees up.
+// Sorts of different batches run on kSortStreams streams at once.  Each
+// batch's partition kernel is a cooperative launch on 1/kSortStreams of the
+// resident CTAs, so the partition grids of all streams fit on the GPU
+// together whatever order their CTAs are dispatched in.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -36,7 +40,9 @@
 
 namespace {
 
-constexpr int kSlots = 3;  // batches in flight
+constexpr int kSlots = 4;        // batches in flight
+constexpr int kSortStreams = 2;  // batches sorting at once
+constexpr int kWindow = 256;     // waiting requests scanned for a batch's group
 
 double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -82,7 +88,8 @@ struct turtle_server {
   long long budget = 0;
   int maxBatchRequests = 4096;
   long long maxBatchKeys = 32ll << 20;
-  cudaStream_t sIn = nullptr, sSort = nullptr, sOut = nullptr;
+  cudaStream_t sIn = nullptr, sOut = nullptr;
+  cudaStream_t sSort[kSortStreams] = {};
   cudaMemPool_t pool = nullptr;  // the server's own stream-ordered pool (keeps freed batches)
   int grid[9][2] = {};
   Slot slots[kSlots];
@@ -123,6 +130,15 @@ void fail_request(turtle_server* s, Request* r, turtle_status st) {
   s->failed++;
 }
 
+// Partition CTAs of a batch: at most 1/kSortStreams of the resident grid (so
+// the cooperative grids of all sort streams are co-resident together), less
+// when the tuned configuration asks for a smaller grid.
+int batch_grid(const turtle_server* s, const Batch* b) {
+  const int full = s->grid[b->width][b->hasIdx ? 1 : 0];
+  const int div = std::max(kSortStreams, b->args.gridDiv > 0 ? b->args.gridDiv : 1);
+  return std::max(1, full / div);
+}
+
 // Launch a formed batch into slot `slot` (called with the lock released: the
 // batch and slot are owned by the worker thread).
 turtle_status launch_batch(turtle_server* s, Batch* b) {
@@ -160,15 +176,13 @@ turtle_status launch_batch(turtle_server* s, Batch* b) {
   b->args = turtle::bind_args(keys, idx, keysB, idxB, ws, b->lay, offs, num, b->total,
                               b->dtype, turtle::kRuleAuto,
                               turtle::tune_lookup(b->width, b->hasIdx, b->total));
-  cudaStreamWaitEvent(s->sSort, sl.inDone, 0);
-  cudaMemsetAsync(b->args.ctrl, 0, sizeof(turtle::Control), s->sSort);
-  e = turtle::kernels_launch_persistent(b->width, b->hasIdx, b->args,
-                                        std::max(1, s->grid[b->width][b->hasIdx ? 1 : 0] / b->args.gridDiv),
-                                        s->sSort);
+  cudaStream_t ss = s->sSort[b->slot % kSortStreams];
+  cudaStreamWaitEvent(ss, sl.inDone, 0);
+  cudaMemsetAsync(b->args.ctrl, 0, sizeof(turtle::Control), ss);
+  e = turtle::kernels_launch_persistent(b->width, b->hasIdx, b->args, batch_grid(s, b), ss);
   if (e != cudaSuccess) { cudaGetLastError(); return TURTLE_ERR_CUDA; }
-  cudaMemcpyAsync(sl.hCtrl, b->args.ctrl, sizeof(turtle::Control), cudaMemcpyDeviceToHost,
-                  s->sSort);
-  cudaEventRecord(sl.sortDone, s->sSort);
+  cudaMemcpyAsync(sl.hCtrl, b->args.ctrl, sizeof(turtle::Control), cudaMemcpyDeviceToHost, ss);
+  cudaEventRecord(sl.sortDone, ss);
   // copy out
   cudaStreamWaitEvent(s->sOut, sl.sortDone, 0);
   for (Request* r : b->reqs) {
@@ -197,13 +211,13 @@ turtle_status finish_batch(turtle_server* s, Batch* b) {
       break;
     }
     b->args.resume = 1;
-    cudaError_t e = turtle::kernels_launch_persistent(
-        b->width, b->hasIdx, b->args,
-        std::max(1, s->grid[b->width][b->hasIdx ? 1 : 0] / b->args.gridDiv), s->sSort);
+    cudaStream_t ss = s->sSort[b->slot % kSortStreams];
+    cudaError_t e = turtle::kernels_launch_persistent(b->width, b->hasIdx, b->args,
+                                                      batch_grid(s, b), ss);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(sl.hCtrl, b->args.ctrl, sizeof(turtle::Control),
-                          cudaMemcpyDeviceToHost, s->sSort);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->sSort);
+                          cudaMemcpyDeviceToHost, ss);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ss);
     if (e != cudaSuccess) {
       cudaGetLastError();
       st = TURTLE_ERR_CUDA;
@@ -214,15 +228,16 @@ turtle_status finish_batch(turtle_server* s, Batch* b) {
   // copy the finished result again
   if (rounds > 0 && st == TURTLE_OK && sl.hCtrl->error == 0) {
     cudaError_t e = cudaSuccess;
+    cudaStream_t ss = s->sSort[b->slot % kSortStreams];
     for (Request* r : b->reqs) {
       if (r->n <= 0 || e != cudaSuccess) continue;
       e = cudaMemcpyAsync(r->hostKeys, b->dev + r->offset * b->width, (size_t)r->n * b->width,
-                          cudaMemcpyDeviceToHost, s->sSort);
+                          cudaMemcpyDeviceToHost, ss);
       if (e == cudaSuccess && b->hasIdx)
         e = cudaMemcpyAsync(r->hostIdx, (const int*)b->args.idxA + r->offset, (size_t)r->n * 4,
-                            cudaMemcpyDeviceToHost, s->sSort);
+                            cudaMemcpyDeviceToHost, ss);
     }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->sSort);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ss);
     if (e != cudaSuccess) {
       cudaGetLastError();
       st = TURTLE_ERR_CUDA;
@@ -285,10 +300,15 @@ void worker_loop(turtle_server* s) {
         b->dtype = head->dtype;
         b->width = head->width;
         b->hasIdx = hasIdx;
-        // consecutive waiting requests of the head's group, within limits
-        for (auto it = s->waiting.begin(); it != s->waiting.end();) {
+        // requests of the head's group among the first kWindow waiting ones,
+        // in arrival order, within the batch limits; others keep their place
+        int scanned = 0;
+        for (auto it = s->waiting.begin(); it != s->waiting.end() && scanned < kWindow; ++scanned) {
           Request* r = *it;
-          if (r->dtype != b->dtype || (r->hostIdx != nullptr) != hasIdx) break;
+          if (r->dtype != b->dtype || (r->hostIdx != nullptr) != hasIdx) {
+            ++it;
+            continue;
+          }
           if ((long long)b->reqs.size() >= s->maxBatchRequests) break;
           if (!b->reqs.empty() && b->total + r->n > s->maxBatchKeys) break;
           const size_t need = batch_bytes(b->width, hasIdx, b->total + r->n,
@@ -386,7 +406,8 @@ turtle_status turtle_server_create(int device, int64_t hbm_budget_bytes, int max
     }
   }
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->sIn, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->sSort, cudaStreamNonBlocking);
+  for (int k = 0; k < kSortStreams && e == cudaSuccess; ++k)
+    e = cudaStreamCreateWithFlags(&s->sSort[k], cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->sOut, cudaStreamNonBlocking);
   for (int k = 0; k < kSlots && e == cudaSuccess; ++k) {
     Slot& sl = s->slots[k];
@@ -503,7 +524,8 @@ turtle_status turtle_server_destroy(turtle_server* s) {
   if (s->worker.joinable()) s->worker.join();
   cudaSetDevice(s->device);
   if (s->sIn) cudaStreamSynchronize(s->sIn);
-  if (s->sSort) cudaStreamSynchronize(s->sSort);
+  for (cudaStream_t ss : s->sSort)
+    if (ss) cudaStreamSynchronize(ss);
   if (s->sOut) cudaStreamSynchronize(s->sOut);
   for (int k = 0; k < kSlots; ++k) {
     Slot& sl = s->slots[k];
@@ -515,7 +537,8 @@ turtle_status turtle_server_destroy(turtle_server* s) {
   }
   if (s->pool) cudaMemPoolDestroy(s->pool);
   if (s->sIn) cudaStreamDestroy(s->sIn);
-  if (s->sSort) cudaStreamDestroy(s->sSort);
+  for (cudaStream_t ss : s->sSort)
+    if (ss) cudaStreamDestroy(ss);
   if (s->sOut) cudaStreamDestroy(s->sOut);
   for (auto& kv : s->all) delete kv.second;
   cudaGetLastError();

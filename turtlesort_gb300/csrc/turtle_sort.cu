@@ -1349,7 +1349,7 @@ template <typename U, bool kIdx, int kV, class LW>
 __device__ __forceinline__ void leaf_words_sort(const SortArgs& a,
                                                 typename LeafCfg<U, kIdx, kV>::Smem& sm, int P,
                                                 int li, int last,
-                                                typename KeyCfg<U>::KT lo) {
+                                                typename KeyCfg<U>::KT lo, int sh) {
   using KT = typename KeyCfg<U>::KT;
   using W = typename LW::W;
   constexpr int kItems = LeafCfg<U, kIdx, kV>::kItems;
@@ -1368,7 +1368,7 @@ __device__ __forceinline__ void leaf_words_sort(const SortArgs& a,
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
       const int j = q + i * P;
-      words[wpad<W>(region + j)] = j < n ? LW::make(lk[i], lo, j) : LW::sent();
+      words[wpad<W>(region + j)] = j < n ? LW::make(lk[i], lo, j, sh) : LW::sent();
     }
   }
   if (q == 0) sm.glo[g] = lo;
@@ -1383,8 +1383,8 @@ __device__ __forceinline__ void leaf_words_sort(const SortArgs& a,
     const KT flip = (KT)a.flip;
     for (int j = q; j < d.n; j += P) {
       const W w = words[wpad<W>(region + j)];
-      kstore<U, KT>(dst, d.start + j, (KT)LW::key(w, base), flip);
-      if (kIdx) dstI[d.start + j] = sm.idx[region + LW::pos(w)];
+      kstore<U, KT>(dst, d.start + j, (KT)LW::key(w, base, sh), flip);
+      if (kIdx) dstI[d.start + j] = sm.idx[region + LW::pos(w, sh)];
     }
   }
 }
@@ -1455,17 +1455,20 @@ __device__ void sort_leaf_group(const SortArgs& a, int cls, int first, int last,
     }
   }
   const unsigned long long range = d.n > 0 ? (unsigned long long)(tmax - tmin) : 0ull;
+  // positions of a group need log2(P * kItems) bits
+  int sh = 0;
+  while ((1 << sh) < P * kItems) ++sh;
   using Narrow = RangeWord<KT, uint32_t, kIdx>;
   using Mid = RangeWord<KT, uint64_t, kIdx>;
   using Full = FullWord<U, kIdx>;
   // 8/16-bit keys and 32-bit keys without ids already sort 32-bit words
   constexpr bool kNarrowOpt = !(sizeof(U) <= 2 || (sizeof(U) == 4 && !kIdx));
-  if (kNarrowOpt && __syncthreads_and(range <= Narrow::kMaxRange)) {
-    leaf_words_sort<U, kIdx, kV, Narrow>(a, sm, P, li, last, tmin);
-  } else if (sizeof(U) == 8 && kIdx && __syncthreads_and(range <= Mid::kMaxRange)) {
-    leaf_words_sort<U, kIdx, kV, Mid>(a, sm, P, li, last, tmin);
+  if (kNarrowOpt && __syncthreads_and(range <= Narrow::max_range(sh))) {
+    leaf_words_sort<U, kIdx, kV, Narrow>(a, sm, P, li, last, tmin, sh);
+  } else if (sizeof(U) == 8 && kIdx && __syncthreads_and(range <= Mid::max_range(sh))) {
+    leaf_words_sort<U, kIdx, kV, Mid>(a, sm, P, li, last, tmin, sh);
   } else {
-    leaf_words_sort<U, kIdx, kV, Full>(a, sm, P, li, last, tmin);
+    leaf_words_sort<U, kIdx, kV, Full>(a, sm, P, li, last, tmin, sh);
   }
   __syncthreads();
 }
