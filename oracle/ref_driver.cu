@@ -61,7 +61,7 @@ int run_sort(const std::string& name, long long n, bool ids, int reps, const std
   }
   // capacity of at least 64: StartSorting copies two task pairs (4 ints)
   // into task buffers of maxN ints even for a single task
-  // (turtle-sort.cuh:172), which fails for maxN < 4
+  // (turtle-sort.cuh:174), which fails for maxN < 4
   Turtle::TurtleSort<T> sorter((int)std::max<long long>(n, 64));
   std::vector<T> firstK;
   std::vector<int> firstI;
