@@ -576,13 +576,9 @@ __device__ __forceinline__ void scatter31_tile_warp(const SortArgs& a, int pass,
     for (int i = 0; i < kItems; ++i) {
       const int e = ch * kWCH + 32 * i + lane;
       const unsigned k = (inner || (e >= rlo && e < rhi)) ? (unsigned)ws.pc[b][32 * i + lane] : 31u;
-      // lanes of the same class: one vote per class bit
-      unsigned peers = 0xffffffffu;
-#pragma unroll
-      for (int bit = 0; bit < 5; ++bit) {
-        const unsigned m = __ballot_sync(kFull, (k >> bit) & 1u);
-        peers &= ((k >> bit) & 1u) ? m : ~m;
-      }
+      // lanes of the same class (one match instruction; measured a little
+      // faster than one vote per class bit)
+      const unsigned peers = __match_any_sync(kFull, k);
       const int base = ws.t.cnt[k];
       const unsigned r = (unsigned)(base + __popc(peers & lt));
       __syncwarp();
