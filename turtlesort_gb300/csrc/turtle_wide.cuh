@@ -490,7 +490,7 @@ __device__ __forceinline__ void wide_bulk_issue(typename Persist<U, kIdx>::WarpA
 // classes come from COUNT (one byte per key, bulk-copied with the keys and
 // ids).  Items are lane-strided (item i of lane l is chunk element 32i + l),
 // so ranking them item by item keeps memory order: the lanes of one class
-// are found with one vote per class bit, and a per-warp running count per
+// are found with one match instruction, and a per-warp running count per
 // class gives the rank.  The class starts come from a lane scan of the chunk's
 // class totals.  Lane k also watches the sample positions of grandchild class
 // k and copies the staged key written there into the new segment's samples.
