@@ -11,15 +11,19 @@ full int32 range, with an int32 index payload (= position); sorted keys/s.
   e2e     the same sort through the reference-facing host API
           (turtle_start + turtle_sync: pinned host buffers, H2D copies,
           sort, D2H copies), wall clock per step.
-  roofline  two-pass HBM bound: 4 * n * (4 B key + 4 B id) algorithmic bytes
-          per sort over the measured HBM copy bandwidth.
+  roofline  the dominant kernel of the form the tuned table picks: the radix
+          form's digit-pass kernel (one read + one write of keys and ids per
+          launch, 2 * n * 8 B) or the partition kernel (charged half of the
+          two-pass bound), over its average launch time from CUDA events;
+          sort_frac: the sort's two-pass bound 4 * n * (4 B key + 4 B id)
+          over the step time.  All against the measured HBM copy bandwidth.
   cpu_baseline  the oracle port of the reference algorithm on all host cores,
           plus std::sort (1 thread) and __gnu_parallel::sort on a sample.
 
 `--impl reference` times the reference algorithm's CPU restatement (the
-oracle port; the reference has no CPU implementation of its own and its GPU
-code cannot be built for the Arm GPU host from this image) on the same
-workload, and prints the same JSON shape with "impl": "reference".
+oracle port: the reference has no CPU implementation of the path; its CUDA
+code is built on the GPU host only to pin parity, by oracle/ref_build.sh) on
+the same workload, and prints the same JSON shape with "impl": "reference".
 """
 from __future__ import annotations
 
@@ -52,13 +56,13 @@ def peaks() -> tuple[float, str]:
     return 6800.0, "fallback"
 
 
-def profile_traffic(n: int) -> tuple[float | None, str | None]:
-    """DRAM bytes (read + write) per launch of the partition kernel and the
-    ncu summary they come from, for the workload size the figure was scaled
-    to (profiles/traffic.json); (None, None) for other sizes."""
+def profile_traffic(n: int, kernel: str) -> tuple[float | None, str | None]:
+    """DRAM bytes (read + write) per launch of `kernel` and the ncu summary
+    they come from, for the workload size the figure was scaled to
+    (profiles/traffic.json); (None, None) for other sizes."""
     p = ROOT / "profiles" / "traffic.json"
     try:
-        e = json.loads(p.read_text())["persistent_sort_kernel"]
+        e = json.loads(p.read_text())[kernel]
     except Exception:
         return None, None
     if int(e.get("bench_n", -1)) != n:
@@ -223,6 +227,8 @@ def run_gpu(args) -> None:
     d_k = torch.empty_like(d_src_k)
     d_i = torch.empty_like(d_src_i)
     sorter = ts.TurtleSort(np.int32, n, compress=False, track_index=True, device=local)
+    if args.form != "auto":
+        sorter.set_pivot_rule(args.form)
     stream = torch.cuda.Stream(device=dev)
     sh = stream.cuda_stream
 
@@ -262,9 +268,13 @@ def run_gpu(args) -> None:
     sorter.status(sh)
     launches = sorter.launches - launches0
     nk, part_ms, leaf_ms = sorter.kernel_times(args.steps)
+    _, setup_ms, pass_ms = sorter.pass_times(args.steps)
     sorter.time_kernels(False)
     part_ms /= max(nk, 1)
     leaf_ms /= max(nk, 1)
+    setup_ms /= max(nk, 1)
+    pass_ms /= max(nk, 1)
+    form, levels = sorter.last_form, sorter.last_levels
     ms = [a.elapsed_time(b) for a, b in events]
     tot_ms = sum(ms)
     tot_ms = max_over_ranks(tot_ms, dist, dev)
@@ -310,13 +320,31 @@ def run_gpu(args) -> None:
     if rank != 0:
         return
     peak, peak_kind = peaks()
-    # two-pass bound of the sort: read + write keys and ids twice; each of the
-    # two kernels (partition, leaf) is charged one of the passes
+    # two-pass bound of the sort: read + write keys and ids twice
     alg_bytes = 4.0 * n * (4 + 4)
-    part_bytes = alg_bytes / 2
-    achieved = part_bytes / (part_ms / 1e3) / 1e9
     sort_achieved = alg_bytes / (ms_step / 1e3) / 1e9
-    traffic, traffic_src = profile_traffic(n)
+    if form == "radix":
+        # one launch per digit that moves keys; each reads and writes keys and ids once
+        launch_bytes = 2.0 * n * (4 + 4)
+        kernel_ms = pass_ms / max(levels, 1)
+        kernel = f"radix_pass_kernel<uint32_t,true> ({levels} launches per sort, one per digit)"
+        note = "one read + one write of keys and ids (2*n*8 B) per digit pass"
+        traffic, traffic_src = profile_traffic(n, "radix_pass_kernel")
+        split = {"kernel_ms": kernel_ms, "passes_ms": pass_ms,
+                 "histogram_and_plan_ms": setup_ms, "finish_ms": leaf_ms}
+        overlap = ("none: the radix form finishes every key in its last pass, so the "
+                   "result is copied back after the sort")
+    else:
+        # the two kernels (partition, leaf) are charged one pass each
+        launch_bytes = alg_bytes / 2
+        kernel_ms = part_ms
+        kernel = "persistent_sort_kernel<uint32_t,true> (one launch per sort)"
+        note = "one read + one write of keys and ids (2*n*8 B), half of the sort's two-pass bound"
+        traffic, traffic_src = profile_traffic(n, "persistent_sort_kernel")
+        split = {"kernel_ms": kernel_ms, "leaf_kernel_ms": leaf_ms}
+        overlap = ("leaf phase in position slices; each finished slice is copied to the "
+                   "host while later slices sort")
+    achieved = launch_bytes / (kernel_ms / 1e3) / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
@@ -330,11 +358,9 @@ def run_gpu(args) -> None:
                      "frac": achieved / peak, "traffic": traffic,
                      "traffic_source": traffic_src,
                      "peak_source": f"{peak_kind} hbm_gbs",
-                     "kernel": "persistent_sort_kernel<uint32_t,true> (one launch per sort)",
-                     "algorithmic_bytes_per_launch": part_bytes,
-                     "algorithmic_bytes_note": "one read + one write of keys and ids (2*n*8 B), "
-                                               "half of the sort's two-pass bound 4*n*8 B",
-                     "kernel_ms": part_ms, "leaf_kernel_ms": leaf_ms,
+                     "kernel": kernel, "form": form,
+                     "algorithmic_bytes_per_launch": launch_bytes,
+                     "algorithmic_bytes_note": note, **split,
                      "sort_achieved": sort_achieved, "sort_frac": sort_achieved / peak},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 8,
                 "d2h_bytes_per_step": n * 8,
@@ -343,8 +369,7 @@ def run_gpu(args) -> None:
                 "ms_min_median_max": [1e3 * min(e2e_t), 1e3 * sorted(e2e_t)[len(e2e_t) // 2],
                                       1e3 * max(e2e_t)],
                 "gpu_launches_per_step": e2e_launches / len(e2e_t),
-                "overlap": "leaf phase in position slices; each finished slice is copied to the "
-                           "host while later slices sort"},
+                "overlap": overlap},
         "tuning": {"table": ts.tuning_source(),
                    "config": ts.tuning_lookup(np.int32, True, n),
                    "tuned_ms_per_step": ms_step,
@@ -373,18 +398,17 @@ def main() -> None:
                     help="keys per sort (--keys also works under torchrun)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--clocks-csv", default=None)
+    ap.add_argument("--form", default="auto", choices=["auto", "radix", "two_level", "sampled"],
+                    help="pass form of the sorts (auto: the tuned table's)")
     ap.add_argument("--workload", default="sort64m",
                     choices=["sort64m", "plain12m", "sweep", "multisort", "batched", "wide",
                              "floats", "serving"],
                     help="sort64m (default) is the headline line; the others print their own")
     ap.add_argument("--requests", type=int, default=20000, help="serving: requests in the stream")
     ap.add_argument("--rate", type=float, default=0.0,
-                    help="serving: Poisson arrivals per second (0: 60%% of the closed-loop rate)")
-    ap.add_argument("--outstanding", type=int, default=64,
-                    help="serving: requests in flight in the closed-loop run")
-    ap.add_argument("--arena-gb", type=int, default=8, help="serving: pinned host arena (GiB)")
-    ap.add_argument("--serial-sample", type=int, default=1000,
-                    help="serving: requests in the serial StartSorting baseline")
+                    help="serving: Poisson arrivals per second (0: 60%% of the saturated rate)")
+    ap.add_argument("--arena-gb", type=int, default=12,
+                    help="serving: pinned host arena that one wave of requests fills (GiB)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3

@@ -118,9 +118,12 @@ def _sort_line(args, name, keys, idx, dtype_name, note=""):
     n = keys.size
     width = keys.dtype.itemsize
     with ts.TurtleSort(keys.dtype, n, track_index=idx is not None) as s:
+        if getattr(args, "form", "auto") != "auto":
+            s.set_pivot_rule(args.form)
         ms, pm, lm = _device_sort_times(torch, s, keys, idx, args.steps, args.warmup)
         e2e = _e2e_sort_times(s, keys, idx, args.steps, args.warmup)
         levels = s.last_levels
+        form = s.last_form
     per = width + (4 if idx is not None else 0)
     alg = 4.0 * n * per
     _line(f"sorted keys/s ({name}, device-resident)", n / (ms / 1e3), "keys/s", args,
@@ -128,7 +131,9 @@ def _sort_line(args, name, keys, idx, dtype_name, note=""):
            "note": note},
           {"dtype": dtype_name, "ms_per_step": ms,
            "roofline_sort": {"algorithmic_bytes": alg, "achieved_gbs": alg / (ms / 1e3) / 1e9},
-           "kernel_ms": {"partition": pm, "leaf": lm},
+           "form": form,
+           "kernel_ms": {"partition": pm, "leaf": lm} if form != "radix" else
+                        {"histogram_plan_passes": pm, "finish": lm},
            "e2e": {"value": n / e2e, "unit": "keys/s", "h2d_bytes_per_step": n * per,
                    "d2h_bytes_per_step": n * per},
            "levels": levels})
@@ -280,52 +285,6 @@ def batched(args):
                "speedup_vs_per_array": (num / e2e) * per_array})
 
 
-class _Arena:
-    """First-fit allocator over one pinned host buffer (16-byte blocks)."""
-
-    def __init__(self, torch, nbytes):
-        self.t = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
-        self.a = self.t.numpy()
-        self.free = [(0, nbytes)]
-        self.cv = threading.Condition()
-
-    def try_alloc(self, nbytes):
-        """(offset, size) of a free block, or None when nothing fits."""
-        nbytes = (nbytes + 15) // 16 * 16
-        with self.cv:
-            for j, (o, sz) in enumerate(self.free):
-                if sz >= nbytes:
-                    self.free[j] = (o + nbytes, sz - nbytes)
-                    if self.free[j][1] == 0:
-                        self.free.pop(j)
-                    return o, nbytes
-            return None
-
-    def alloc(self, nbytes):
-        while True:
-            blk = self.try_alloc(nbytes)
-            if blk is not None:
-                return blk
-            self.wait_release()
-
-    def wait_release(self, timeout=0.05):
-        with self.cv:
-            self.cv.wait(timeout)
-
-    def release(self, o, nbytes):
-        with self.cv:
-            self.free.append((o, nbytes))
-            self.free.sort()
-            merged = []
-            for fo, fs in self.free:
-                if merged and merged[-1][0] + merged[-1][1] == fo:
-                    merged[-1] = (merged[-1][0], merged[-1][1] + fs)
-                else:
-                    merged.append((fo, fs))
-            self.free = merged
-            self.cv.notify_all()
-
-
 _MIX1 = np.uint64(0xBF58476D1CE4E5B9)
 _MIX2 = np.uint64(0x94D049BB133111EB)
 
@@ -366,14 +325,22 @@ def serving(args):
     (20,000 by default) with log-uniform sizes in [1024, 16 * 2^20], dtype
     int32 60% / int64 25% / uint16 15%, half with an int32 index (= position),
     values uniform over each dtype's range (slices of a seeded random pool),
-    HBM budget 64 GB.  Host buffers come from a pinned arena (requests wait
-    for room, as a server's callers would); every result is checked exactly
-    on a thread pool (_check_request).  Runs:
-      closed loop  up to --outstanding requests in flight (throughput);
-      poisson      Poisson arrivals at --rate (default: 60% of the closed-loop
-                   request rate), latency from arrival to completion;
-      serial       one StartSorting + Sync per request for the first
-                   --serial-sample requests (the reference's way to serve)."""
+    HBM budget 64 GB.
+
+    The stream is cut into waves of consecutive requests that fit one pinned
+    host arena (--arena-gb).  Each wave's inputs are written to the arena
+    before its timed region (a server's callers hold their data in memory
+    when they submit), and every result is checked exactly after it
+    (_check_request, on a thread pool), so the timed regions hold only the
+    server's work: the host->device copies, the sorts and the device->host
+    copies.  Three passes over the whole stream:
+      saturated  every request of a wave submitted at once; keys/s = all keys
+                 / the summed wave times (the throughput under full load);
+      poisson    Poisson arrivals at --rate (default: 60% of the saturated
+                 request rate), latency from the scheduled arrival to
+                 completion;
+      serial     one StartSorting + Sync per request, in stream order (the
+                 reference's way to serve: one sort call per array)."""
     import concurrent.futures as cf
     import os
     torch = _torch()
@@ -384,9 +351,9 @@ def serving(args):
     with_idx = rng_u[2 * nreq:3 * nreq] < 0.5
     dtypes = [np.int32, np.int64, np.uint16]
     pool = dg.uniform(np.uint64, 1 << 26, dg.seed_for(4) + 1)  # 512 MiB of random words
+    positions = np.arange(16 << 20, dtype=np.int32)
     keys_total = int(sizes.sum())
-    arena = _Arena(torch, args.arena_gb << 30)
-    checker = cf.ThreadPoolExecutor(max(2, (os.cpu_count() or 4) - 2))
+    workers = cf.ThreadPoolExecutor(max(2, os.cpu_count() or 4))
 
     def request_input(r):
         dt = np.dtype(dtypes[dts[r]])
@@ -395,163 +362,159 @@ def serving(args):
         off = int((r * 7919 * 7919) % (pool.size - words))
         return pool[off: off + words].view(dt)[:n]
 
-    def need(r):
+    def spans(r):
+        """(key bytes, id bytes) of request r, each rounded up to 16 bytes."""
         n = int(sizes[r])
-        return n * np.dtype(dtypes[dts[r]]).itemsize + 16 + (4 * n if with_idx[r] else 0)
+        kb = (n * np.dtype(dtypes[dts[r]]).itemsize + 15) // 16 * 16
+        return kb, (4 * n + 15) // 16 * 16 if with_idx[r] else 0
 
-    def stage(r, blk=None):
-        """Pinned key / id buffers of request r, filled with its input."""
-        dt = np.dtype(dtypes[dts[r]])
-        n = int(sizes[r])
-        kb = n * dt.itemsize
-        ib = 4 * n if with_idx[r] else 0
-        o, sz = blk if blk is not None else arena.alloc(kb + 16 + ib)
-        kv = arena.a[o: o + kb].view(dt)
-        kv[:] = request_input(r)
-        iv = None
-        if ib:
-            io = o + (kb + 15) // 16 * 16
-            iv = arena.a[io: io + ib].view(np.int32)
-            iv[:] = np.arange(n, dtype=np.int32)
-        return kv, iv, (o, sz)
+    arena_bytes = args.arena_gb << 30
+    waves = []  # [lo, hi) request ranges whose buffers fit the arena together
+    lo, used = 0, 0
+    for r in range(nreq):
+        kb, ib = spans(r)
+        if used + kb + ib > arena_bytes and r > lo:
+            waves.append((lo, r))
+            lo, used = r, 0
+        used += kb + ib
+    waves.append((lo, nreq))
+    arena_t = torch.empty(arena_bytes, dtype=torch.uint8, pin_memory=True)
+    arena = arena_t.numpy()
+
+    def stage(lo, hi):
+        """Pinned key / id buffers of requests [lo, hi), filled with their inputs."""
+        bufs, o = [], 0
+        for r in range(lo, hi):
+            kb, ib = spans(r)
+            n = int(sizes[r])
+            kv = arena[o: o + kb].view(dtypes[dts[r]])[:n]
+            iv = arena[o + kb: o + kb + ib].view(np.int32)[:n] if ib else None
+            bufs.append((kv, iv))
+            o += kb + ib
+
+        def fill(j):
+            kv, iv = bufs[j]
+            kv[:] = request_input(lo + j)
+            if iv is not None:
+                iv[:] = positions[: iv.size]
+        list(workers.map(fill, range(hi - lo)))
+        return bufs
 
     failures = []
 
-    def verify(r, kv, iv, blk):
-        err = _check_request(request_input(r), kv, iv)
-        if err:
-            failures.append((r, err))
-        arena.release(*blk)
+    def check(lo, bufs, what):
+        def one(j):
+            kv, iv = bufs[j]
+            return _check_request(request_input(lo + j), kv, iv)
+        for j, err in enumerate(workers.map(one, range(len(bufs)))):
+            if err:
+                failures.append((what, lo + j, err))
 
     srv = ts.TurtleServer(hbm_budget_bytes=64 << 30)
-    # warm-up (kernels, pool), untimed
-    for r in range(min(8, nreq)):
-        kv, iv, blk = stage(r)
+    bufs = stage(0, min(8, nreq))  # warm-up (kernels, memory pool), untimed
+    for kv, iv in bufs:
         srv.wait(srv.submit(kv, iv))
-        arena.release(*blk)
 
-    def closed_loop(limit):
-        inflight = []
-        lat = []
-        checks = []
-        t0 = time.perf_counter()
-        def retire():
-            rr, tk, k2, i2, b2 = inflight.pop(0)
-            lat.append(srv.wait(tk))
-            checks.append(checker.submit(verify, rr, k2, i2, b2))
-
-        for r in range(nreq):
-            blk = arena.try_alloc(need(r))
-            while blk is None:  # the arena is full: retire the oldest, or wait for a check
-                if inflight:
-                    retire()
-                else:
-                    arena.wait_release()
-                blk = arena.try_alloc(need(r))
-            kv, iv, blk = stage(r, blk)
-            inflight.append((r, srv.submit(kv, iv), kv, iv, blk))
-            while len(inflight) >= limit:
-                retire()
-        for rr, tk, k2, i2, b2 in inflight:
-            lat.append(srv.wait(tk))
-            checks.append(checker.submit(verify, rr, k2, i2, b2))
-        t = time.perf_counter() - t0
-        for c in checks:
-            c.result()
-        return t, lat
-
+    # saturated
     st0 = srv.stats()
-    t_sat, _ = closed_loop(args.outstanding)
+    t_sat = 0.0
+    for lo, hi in waves:
+        bufs = stage(lo, hi)
+        t0 = time.perf_counter()
+        tickets = [srv.submit(kv, iv) for kv, iv in bufs]
+        for tk in tickets:
+            srv.wait(tk)
+        t_sat += time.perf_counter() - t0
+        check(lo, bufs, "saturated")
     st1 = srv.stats()
     sat_kps = keys_total / t_sat
     sat_rps = nreq / t_sat
+
     # Poisson arrivals
     rate = args.rate if args.rate > 0 else 0.6 * sat_rps
     gaps = -np.log(np.maximum(rng_u[3 * nreq:4 * nreq], 1e-12)) / rate
-    arrivals = np.cumsum(gaps)
-    lat = [0.0] * nreq
-    pending = []
-    cv = threading.Condition()
-    done_flag = [False]
+    lat = np.zeros(nreq)
+    t_pois = 0.0
+    for lo, hi in waves:
+        bufs = stage(lo, hi)
+        arrive = np.cumsum(gaps[lo:hi]) - gaps[lo]  # the wave's first request arrives at 0
+        queue, cv = [], threading.Condition()
 
-    def waiter():
-        while True:
+        def waiter(count=hi - lo):
+            for _ in range(count):
+                with cv:
+                    while not queue:
+                        cv.wait()
+                    r, tk, late = queue.pop(0)
+                lat[r] = late + srv.wait(tk)  # scheduled arrival -> completion
+
+        th = threading.Thread(target=waiter)
+        th.start()
+        t_start = time.perf_counter()
+        for j, (kv, iv) in enumerate(bufs):
+            target = t_start + arrive[j]
+            while time.perf_counter() < target:
+                left = target - time.perf_counter()
+                if left > 2e-3:
+                    time.sleep(left - 1e-3)
+            late = time.perf_counter() - target
+            tk = srv.submit(kv, iv)
             with cv:
-                while not pending and not done_flag[0]:
-                    cv.wait()
-                if not pending and done_flag[0]:
-                    return
-                r, tk, t_arr, kv, iv, blk = pending.pop(0)
-            srv.wait(tk)
-            lat[r] = time.perf_counter() - t_arr
-            checker.submit(verify, r, kv, iv, blk)
-
-    th = threading.Thread(target=waiter)
-    th.start()
-    t_start = time.perf_counter()
-    for r in range(nreq):
-        target = t_start + arrivals[r]
-        now = time.perf_counter()
-        if target > now:
-            time.sleep(target - now)
-        kv, iv, blk = stage(r)
-        tk = srv.submit(kv, iv)
-        with cv:
-            pending.append((r, tk, max(target, t_start), kv, iv, blk))
-            cv.notify_all()
-    with cv:
-        done_flag[0] = True
-        cv.notify_all()
-    th.join()
-    t_pois = time.perf_counter() - t_start
+                queue.append((lo + j, tk, late))
+                cv.notify()
+        th.join()
+        t_pois += time.perf_counter() - t_start
+        check(lo, bufs, "poisson")
     st2 = srv.stats()
     srv.close()
-    checker.shutdown(wait=True)
-    # serial StartSorting + Sync on a sample
-    ns = min(args.serial_sample, nreq)
+
+    # serial StartSorting + Sync, one request at a time
     sorters = {}
     t_serial = 0.0
-    serial_keys = 0
-    for r in range(ns):
-        key = (int(dts[r]), bool(with_idx[r]))
-        if key not in sorters:
-            sorters[key] = ts.TurtleSort(dtypes[dts[r]], 16 << 20, track_index=key[1])
-        kv, iv, blk = stage(r)
-        t0 = time.perf_counter()
-        sorters[key].StartSorting(kv, iv)
-        sorters[key].Sync()
-        t_serial += time.perf_counter() - t0
-        serial_keys += kv.size
-        err = _check_request(request_input(r), kv, iv)
-        if err:
-            failures.append((r, "serial: " + err))
-        arena.release(*blk)
+    for lo, hi in waves:
+        bufs = stage(lo, hi)
+        for j, (kv, iv) in enumerate(bufs):
+            key = (int(dts[lo + j]), iv is not None)
+            if key not in sorters:
+                sorters[key] = ts.TurtleSort(dtypes[key[0]], 16 << 20, track_index=key[1])
+                sorters[key].StartSorting(kv[:1024].copy(), positions[:1024].copy() if key[1] else None)
+                sorters[key].Sync()  # untimed first call (kernel set-up)
+            t0 = time.perf_counter()
+            sorters[key].StartSorting(kv, iv)
+            sorters[key].Sync()
+            t_serial += time.perf_counter() - t0
+        check(lo, bufs, "serial")
     for srt in sorters.values():
         srt.close()
+    workers.shutdown(wait=True)
     if failures:
         raise RuntimeError(f"{len(failures)} requests wrong, first: {failures[:3]}")
-    serial_kps = serial_keys / t_serial
-    lat_ms = np.array(lat) * 1e3
+    serial_kps = keys_total / t_serial
+    lat_ms = lat * 1e3
     batches_sat = st1["batches"] - st0["batches"]
     batches_pois = st2["batches"] - st1["batches"]
-    _line("served keys/s (request stream, continuous batching, closed loop)", sat_kps, "keys/s",
+    wire = int(sum(spans(r)[0] + spans(r)[1] for r in range(nreq)))
+    _line("served keys/s (request stream, continuous batching, saturated)", sat_kps, "keys/s",
           args,
           {"workload": f"{nreq} requests, sizes log-uniform [1024, 16*2^20], int32 60%/int64 "
                        f"25%/uint16 15%, half with int32 ids, HBM budget 64 GB",
-           "requests": nreq, "keys": keys_total, "outstanding": args.outstanding},
-          {"dtype": "mixed", "requests_per_s": sat_rps, "batches": batches_sat,
+           "requests": nreq, "keys": keys_total, "waves": len(waves), "arena_gb": args.arena_gb},
+          {"dtype": "mixed", "requests_per_s": sat_rps, "seconds": t_sat, "batches": batches_sat,
            "requests_per_batch": nreq / max(batches_sat, 1),
            "poisson": {"arrival_rate_per_s": rate, "p50_ms": float(np.percentile(lat_ms, 50)),
                        "p99_ms": float(np.percentile(lat_ms, 99)),
                        "mean_ms": float(lat_ms.mean()), "keys_per_s": keys_total / t_pois,
                        "batches": batches_pois,
                        "requests_per_batch": nreq / max(batches_pois, 1)},
-           "serial_startsorting_keys_per_s": serial_kps,
-           "serial_sample": f"first {ns} requests, one StartSorting + Sync each",
+           "serial_startsorting_keys_per_s": serial_kps, "serial_seconds": t_serial,
            "speedup_vs_serial": sat_kps / serial_kps,
-           "checked": f"all {nreq} requests of both runs and the serial sample, exactly",
-           "e2e": {"value": sat_kps, "unit": "keys/s",
-                   "note": "pinned host buffers; host<->device copies inside every request"}})
+           "checked": f"all {nreq} requests of each of the three passes, exactly",
+           "timed": "server work only: inputs written to pinned buffers before, results "
+                    "checked after each wave's timed region",
+           "e2e": {"value": sat_kps, "unit": "keys/s", "h2d_bytes_per_step": wire,
+                   "d2h_bytes_per_step": wire,
+                   "note": "one step = the whole stream; pinned host buffers, every request's "
+                           "host<->device copies inside the timed region"}})
 
 
 WORKLOADS = {"plain12m": plain12m, "sweep": sweep, "wide": wide, "floats": floats,

@@ -216,12 +216,17 @@ turtle_status turtle_server_destroy(turtle_server* srv);
  *   TURTLE_PIVOTS_TWO_LEVEL  passes that apply two levels at once (31 classes;
  *                            pivots from 63 evenly spaced keys): half the
  *                            passes over the data, more work per key;
- *   TURTLE_PIVOTS_AUTO       (default) two-level passes for sorts of at least
- *                            2^23 keys, the sampled rule for smaller ones. */
+ *   TURTLE_PIVOTS_AUTO       (default) the tuned table's form for the key
+ *                            type and size;
+ *   TURTLE_FORM_RADIX        no pivots: least-significant-digit radix passes
+ *                            over 8-bit digits (one read + one write of keys
+ *                            and ids per digit that varies, plus one histogram
+ *                            read); batched sorts keep a pivot form. */
 #define TURTLE_PIVOTS_REFERENCE 0
 #define TURTLE_PIVOTS_SAMPLED 1
 #define TURTLE_PIVOTS_TWO_LEVEL 2
 #define TURTLE_PIVOTS_AUTO 3
+#define TURTLE_FORM_RADIX 4
 turtle_status turtle_set_pivot_rule(turtle_sorter* s, int rule);
 
 /* ---- introspection ---- */
@@ -232,6 +237,12 @@ int64_t turtle_launch_count(const turtle_sorter* s);
 /* Partition levels run by the last completed sort (after turtle_stream_status
  * or turtle_sync). */
 int turtle_last_levels(const turtle_sorter* s);
+
+/* Form of the last enqueued sort: TURTLE_FORM_RADIX, or the pivot rule its
+ * partition used (TURTLE_PIVOTS_REFERENCE / _SAMPLED / _TWO_LEVEL); for the
+ * radix form turtle_last_levels is the number of digit passes that moved
+ * keys. */
+int turtle_last_form(const turtle_sorter* s);
 
 /* Largest n a sorter of this dtype can be created for (limited by the int32
  * index payload when track_index != 0). */
@@ -276,10 +287,18 @@ turtle_status turtle_debug_time_kernels(turtle_sorter* s, int enable);
  * sorts.  Returns the number of sorts summed (0 if timing is off). */
 int turtle_debug_kernel_times(turtle_sorter* s, int last, double* partition_ms, double* leaf_ms);
 
+/* The partition time of the same sorts split at the start of the partition
+ * kernel (radix form: of the first digit pass): setup_ms = before it (float
+ * map; radix: histogram and plan kernels), pass_ms = the partition kernel
+ * (radix: all digit-pass kernels).  For the radix form partition_ms above
+ * covers histogram, plan and passes, leaf_ms the finish kernel. */
+int turtle_debug_pass_times(turtle_sorter* s, int last, double* setup_ms, double* pass_ms);
+
 /* Where the last sort's device-side error was recorded (valid after
  * turtle_stream_status / turtle_sync): site 1 = grid barrier wait limit,
  * 2 = grid barrier (with leaf work) wait limit, 3 = bulk-copy wait limit,
- * 4 = a work list was full; block = the CTA; info = site detail.  Returns
+ * 4 = a work list was full, 5 = radix look-back wait limit (info = the tile
+ * that gave up); block = the CTA; info = site detail.  Returns
  * the device status word (0 = no error). */
 int turtle_debug_error_site(const turtle_sorter* s, int* site, int* block, int* info);
 
@@ -297,6 +316,13 @@ turtle_status turtle_debug_yield_threshold(turtle_sorter* s, int32_t leaves);
  * grid-barrier wait is shortened; a CTA has no bulk copy in flight there. */
 turtle_status turtle_debug_barrier_polls(turtle_sorter* s, int64_t polls);
 
+/* Testing the radix form's bounded look-back wait: tile `tile` (>= 0) of every
+ * later radix-form digit pass never publishes its look-back words, so the
+ * tiles after it wait until the poll limit (turtle_debug_barrier_polls) and
+ * the sort reports TURTLE_ERR_TIMEOUT without writing; tile < 0 turns it off.
+ * The GPU stays usable: no wait is unbounded and nothing faults. */
+turtle_status turtle_debug_radix_stall(turtle_sorter* s, int64_t tile);
+
 /* ---- launch configuration (autotuning) ----
  *
  * The reference fixes its kernel geometry at compile time
@@ -304,8 +330,8 @@ turtle_status turtle_debug_barrier_polls(turtle_sorter* s, int64_t polls);
  * turtle-multi-sort.cuh:11,13).  Here each sort picks, by key type, index
  * flag and size band, a configuration from a table that the project's tuner
  * (turtlesort_gb300/tune.py) measured on the GPU and compiled into the
- * library: pass form (TURTLE_PIVOTS_SAMPLED one-level or
- * TURTLE_PIVOTS_TWO_LEVEL), partition tile (1 << tile_shift keys, shift
+ * library: pass form (TURTLE_PIVOTS_SAMPLED one-level,
+ * TURTLE_PIVOTS_TWO_LEVEL or TURTLE_FORM_RADIX), partition tile (1 << tile_shift keys, shift
  * 10..12), shared-memory sort geometry (0..3, see turtle_leaf_geometry), leaf
  * cut (segments of at most leaf_cut keys are sorted in shared memory; 1024 up
  * to the geometry's capacity) and partition grid (resident CTAs / grid_div,
@@ -316,15 +342,18 @@ turtle_status turtle_debug_barrier_polls(turtle_sorter* s, int64_t polls);
 turtle_status turtle_set_tuning(turtle_sorter* s, int enable);
 
 /* Pins one configuration for every later sort on this sorter (form < 0
- * returns to the table).  May reallocate the sorter's work lists, after
+ * returns to the table; form TURTLE_FORM_RADIX: plain sorts use the radix
+ * form, batched sorts two-level passes with the other values).  May reallocate the sorter's work lists, after
  * waiting for the device.  TURTLE_ERR_INVALID_ARGUMENT for values outside the
  * ranges above. */
 turtle_status turtle_set_config(turtle_sorter* s, int form, int tile_shift, int leaf_geometry,
                                 int leaf_cut, int grid_div);
 
-/* The table's configuration for n keys: out5 = {form, tile_shift,
- * leaf_geometry, leaf_cut, grid_div}. */
-turtle_status turtle_tuning_lookup(turtle_dtype dtype, int track_index, int64_t n, int32_t* out5);
+/* The table's configuration for n keys: out6 = {form, tile_shift,
+ * leaf_geometry, leaf_cut, grid_div, radix}; radix = 1 when plain sorts of
+ * that size use TURTLE_FORM_RADIX (the other values then configure batched
+ * sorts). */
+turtle_status turtle_tuning_lookup(turtle_dtype dtype, int track_index, int64_t n, int32_t* out6);
 
 /* The table's shared-memory geometry for MultiSort arrays of arr_size keys
  * (-1: none listed; the default geometry is used). */

@@ -5,7 +5,8 @@
   TURTLE_ERR_TIMEOUT (the reference aborts the process on any CUDA error,
   turtle-globals.cuh:18-30), and the next sort on the same sorter must be
   exact.  Only the grid-barrier wait is shortened: a CTA has no bulk copy in
-  flight while it waits there.
+  flight while it waits there.  The radix form's look-back wait is made to
+  run out by a tile that never publishes its words (a flag nothing sets).
 * Device-buffer allocation failures injected on the host: the constructor
   fails with TURTLE_ERR_OUT_OF_MEMORY at each of its buffers in turn and
   leaves no device memory behind (turtle-buffer.cuh:43-57 is the reference's
@@ -72,6 +73,7 @@ def test_device_form_reports_timeout(gpu):
         keys = dg.uniform(np.uint64, n, 99)
         d = torch.from_numpy(keys.view(np.int64).copy()).cuda()
         torch.cuda.synchronize()
+        s.set_pivot_rule("two_level")  # the grid-barrier wait of the partition kernel
         s.barrier_polls(1)
         s.sort_device(d.data_ptr(), None, n, None)
         with pytest.raises(TurtleError) as ei:
@@ -83,6 +85,37 @@ def test_device_form_reports_timeout(gpu):
         s.sort_device(d.data_ptr(), None, n, None)
         s.status(None)
         assert np.array_equal(d.cpu().numpy().view(np.uint64), np.sort(keys))
+    finally:
+        s.close()
+
+
+@pytest.mark.parametrize("stall", [0, 7, 250])
+def test_radix_lookback_timeout_then_recovers(gpu, stall):
+    n = (1 << 20) + 17  # 257 tiles of 4096 keys
+    s = TurtleSort(np.int32, n, track_index=True)
+    try:
+        s.set_pivot_rule("radix")
+        keys = dg.uniform(np.int32, n, 777)
+        idx = np.arange(n, dtype=np.int32)
+        s.barrier_polls(20000)
+        s.radix_stall(stall)
+        k, i = keys.copy(), idx.copy()
+        s.StartSorting(k, i)
+        with pytest.raises(TurtleError) as ei:
+            s.Sync()
+        assert ei.value.status == TIMEOUT
+        status, site, _block, info = s.error_site()
+        assert status == TIMEOUT and site == 5 and info > stall  # a later tile gave up
+        # no wait was unbounded: the sorter sorts exactly again
+        s.radix_stall(-1)
+        s.barrier_polls(0)
+        ek, eidx = _stable(keys, idx)
+        for _ in range(2):
+            k, i = keys.copy(), idx.copy()
+            s.StartSorting(k, i)
+            s.Sync()
+            assert s.last_form == "radix"
+            assert np.array_equal(k, ek) and np.array_equal(i, eidx)
     finally:
         s.close()
 

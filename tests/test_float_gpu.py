@@ -135,6 +135,7 @@ def test_float_overlapped_copies_and_yields():
     it = torch.empty(n, dtype=torch.int32, pin_memory=True)
     kb, ib = kt.numpy(), it.numpy()
     s = TurtleSort(np.float32, n, track_index=True)
+    s.set_pivot_rule("two_level")  # yields are a partition-kernel path
     order = expected_order(x)
     for thresh in (0, 64):
         s.yield_threshold(thresh)

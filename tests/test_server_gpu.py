@@ -173,3 +173,23 @@ def test_server_float_requests():
         assert np.array_equal(k.view(bits), x[order].view(bits)), (x.dtype, x.size)
         if i is not None:
             assert np.array_equal(i, idx[order]), (x.dtype, x.size)
+
+
+def test_serving_workload_small_stream():
+    """The benchmark suite's serving stream at 64 requests: the three passes
+    (saturated, Poisson, serial StartSorting) run and every result is checked
+    exactly inside the workload, which raises on any wrong request."""
+    import json
+    import os
+    import subprocess
+    import sys
+    _torch_cuda()
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--workload", "serving",
+                          "--requests", "64", "--arena-gb", "1"],
+                         cwd=root, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads([s for s in out.stdout.splitlines() if s.startswith("{")][-1])
+    assert line["config"]["requests"] == 64 and line["config"]["waves"] >= 1
+    assert line["value"] > 0 and line["serial_startsorting_keys_per_s"] > 0
+    assert line["checked"].startswith("all 64 requests")

@@ -23,7 +23,7 @@ WIDTH_DTYPE = {1: np.uint8, 2: np.uint16, 4: np.uint32, 8: np.uint64}
 def parse_table():
     text = TABLE.read_text()
     sorts = [tuple(int(x) for x in m.groups()) for m in re.finditer(
-        r"\{(\d+), (\d+), (\d+)LL, \{(\d+), (\d+), (\d+), (\d+), (\d+)\}\}", text)]
+        r"\{(\d+), (\d+), (\d+)LL, \{(\d+), (\d+), (\d+), (\d+), (\d+), (\d+)\}\}", text)]
     multi = [tuple(int(x) for x in m.groups()) for m in re.finditer(
         r"^\s+\{(\d+), (\d+), (\d+), (\d+)\},$", text, re.M)]
     sorts = [r for r in sorts if r[0] != 0]
@@ -33,7 +33,7 @@ def parse_table():
 
 def lookup(lib, width, ids, n):
     import turtlesort_gb300 as ts
-    out = (C.c_int32 * 5)()
+    out = (C.c_int32 * 6)()
     assert lib.turtle_tuning_lookup(ts.dtype_code(WIDTH_DTYPE[width]), int(ids), int(n), out) == 0
     return tuple(out)
 
@@ -60,9 +60,10 @@ def test_leaf_geometries(native_lib):
 
 def test_table_entries_are_valid(native_lib):
     sorts, multi = parse_table()
-    for w, ids, max_n, form, tile, g, cut, gd in sorts:
+    for w, ids, max_n, form, tile, g, cut, gd, radix in sorts:
         assert w in WIDTH_DTYPE and ids in (0, 1) and max_n > 0
         assert form in (1, 2) and 10 <= tile <= 12 and 0 <= g <= 3 and gd in (1, 2, 4)
+        assert radix in (0, 1)
         assert 1024 <= cut <= geometry(native_lib, w, g)[2]
     for key in {(r[0], r[1]) for r in sorts}:
         bands = [r[2] for r in sorts if (r[0], r[1]) == key]
@@ -80,8 +81,8 @@ def test_lookup_returns_the_table(native_lib):
                 # no entry: the compile-time defaults (two-level from 2^23 keys,
                 # 2048-key tiles, geometry 1 at full capacity, whole grid)
                 cap = geometry(native_lib, w, 1)[2]
-                assert lookup(native_lib, w, ids, 1 << 20) == (1, 11, 1, cap, 1)
-                assert lookup(native_lib, w, ids, 1 << 23) == (2, 11, 1, cap, 1)
+                assert lookup(native_lib, w, ids, 1 << 20) == (1, 11, 1, cap, 1, 0)
+                assert lookup(native_lib, w, ids, 1 << 23) == (2, 11, 1, cap, 1, 0)
                 continue
             prev = 0
             for r in rows:

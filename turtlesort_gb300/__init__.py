@@ -214,12 +214,20 @@ class TurtleSort:
     def last_levels(self) -> int:
         return int(self._lib.turtle_last_levels(self._h))
 
+    @property
+    def last_form(self) -> str:
+        """Form of the last enqueued sort: 'radix', 'two_level', 'sampled' or
+        'reference'."""
+        return {0: "reference", 1: "sampled", 2: "two_level", 4: "radix"}.get(
+            int(self._lib.turtle_last_form(self._h)), "none")
+
     def set_pivot_rule(self, rule: str) -> None:
-        """'auto' (default: two-level passes from 2^23 keys up, else 'sampled'),
-        'sampled' (quartiles of 31 evenly spaced keys), 'reference' (the
-        reference's median of start/middle/stop keys) or 'two_level' (passes
-        of two levels, 31 classes); same output."""
-        code = {"reference": 0, "sampled": 1, "two_level": 2, "auto": 3}[rule]
+        """'auto' (default: the tuned table's form), 'sampled' (quartiles of
+        31 evenly spaced keys), 'reference' (the reference's median of
+        start/middle/stop keys), 'two_level' (passes of two levels, 31
+        classes) or 'radix' (LSD passes over 8-bit digits; plain sorts, batched
+        sorts keep a pivot form); same output."""
+        code = {"reference": 0, "sampled": 1, "two_level": 2, "auto": 3, "radix": 4}[rule]
         _check(self._lib.turtle_set_pivot_rule(self._h, code), "set_pivot_rule", self._h)
 
     def error_site(self):
@@ -248,10 +256,11 @@ class TurtleSort:
 
     def set_config(self, form: str, tile_shift: int, geometry: int, leaf_cut: int,
                    grid_div: int = 1) -> None:
-        """Pin a launch configuration: form 'sampled' (one-level passes) or
-        'two_level', tile of 1 << tile_shift keys, shared-memory geometry
-        0..3, leaf cut, partition grid divisor 1/2/4."""
-        code = {"sampled": 1, "two_level": 2}[form]
+        """Pin a launch configuration: form 'sampled' (one-level passes),
+        'two_level' or 'radix' (LSD digit passes: the other values then apply
+        only to batched sorts), tile of 1 << tile_shift keys, shared-memory
+        geometry 0..3, leaf cut, partition grid divisor 1/2/4."""
+        code = {"sampled": 1, "two_level": 2, "radix": 4}[form]
         _check(self._lib.turtle_set_config(self._h, code, int(tile_shift), int(geometry),
                                            int(leaf_cut), int(grid_div)), "set_config", self._h)
 
@@ -265,20 +274,34 @@ class TurtleSort:
         _check(self._lib.turtle_debug_barrier_polls(self._h, int(polls)), "barrier_polls",
                self._h)
 
+    def radix_stall(self, tile: int) -> None:
+        """Testing: tile ``tile`` of every later radix digit pass never
+        publishes its look-back words, so the sort runs into the poll limit and
+        reports TURTLE_ERR_TIMEOUT; a negative tile turns this off."""
+        _check(self._lib.turtle_debug_radix_stall(self._h, int(tile)), "radix_stall", self._h)
+
     def kernel_times(self, last: int):
         """(sorts, partition_ms, leaf_ms) summed over the last `last` timed sorts."""
         pm, lm = C.c_double(), C.c_double()
         n = self._lib.turtle_debug_kernel_times(self._h, int(last), C.byref(pm), C.byref(lm))
         return int(n), float(pm.value), float(lm.value)
 
+    def pass_times(self, last: int):
+        """(sorts, setup_ms, pass_ms) summed over the last `last` timed sorts:
+        the partition time split where the partition kernel (radix form: the
+        first digit pass) starts."""
+        su, pm = C.c_double(), C.c_double()
+        n = self._lib.turtle_debug_pass_times(self._h, int(last), C.byref(su), C.byref(pm))
+        return int(n), float(su.value), float(pm.value)
+
 
 def tuning_lookup(dtype, track_index: bool, n: int) -> dict:
     """The tuned configuration the table gives a sort of n keys."""
-    out = (C.c_int32 * 5)()
+    out = (C.c_int32 * 6)()
     _check(load_library().turtle_tuning_lookup(dtype_code(dtype), int(track_index), int(n), out),
            "tuning_lookup")
     return {"form": out[0], "tile_shift": out[1], "geometry": out[2], "leaf_cut": out[3],
-            "grid_div": out[4]}
+            "grid_div": out[4], "radix": out[5]}
 
 
 def leaf_geometry(dtype, g: int) -> dict:

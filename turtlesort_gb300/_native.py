@@ -45,6 +45,7 @@ SIGNATURES = [
     ("turtle_stream_status", _I, [_P, _P]),
     ("turtle_launch_count", _I64, [_P]),
     ("turtle_last_levels", _I, [_P]),
+    ("turtle_last_form", _I, [_P]),
     ("turtle_max_elements", _I64, [_I, _I]),
     ("turtle_smem_capacity", _I64, [_I, _I]),
     ("turtle_status_string", C.c_char_p, [_I]),
@@ -58,9 +59,11 @@ SIGNATURES = [
     ("turtle_set_pivot_rule", _I, [_P, _I]),
     ("turtle_debug_time_kernels", _I, [_P, _I]),
     ("turtle_debug_kernel_times", _I, [_P, _I, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    ("turtle_debug_pass_times", _I, [_P, _I, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("turtle_debug_error_site", _I, [_P, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I)]),
     ("turtle_debug_yield_threshold", _I, [_P, C.c_int32]),
     ("turtle_debug_barrier_polls", _I, [_P, _I64]),
+    ("turtle_debug_radix_stall", _I, [_P, _I64]),
     ("turtle_set_tuning", _I, [_P, _I]),
     ("turtle_set_config", _I, [_P, _I, _I, _I, _I, _I]),
     ("turtle_tuning_lookup", _I, [_I, _I, _I64, _P]),

@@ -78,7 +78,8 @@ struct turtle_sorter {
   bool overlapped = false;  // this StartSorting's result copies are queued on copyStream
   bool yielded = false;     // the partition yielded: those copies may be stale
   int leafYield = 0;        // test threshold for yields (0: default)
-  long long barrierPolls = 0;  // test limit of the grid-barrier wait (0: default)
+  long long barrierPolls = 0;  // test limit of the grid-barrier / look-back wait (0: default)
+  long long radixStall = 0;    // test: radix tile + 1 that never publishes (0: none)
   // launch configuration: the tuned table (default), the compile-time
   // defaults, or one pinned configuration
   bool tuning = true;
@@ -87,7 +88,8 @@ struct turtle_sorter {
   // optional kernel timing: events around the two launches of each sort
   static constexpr int kRing = 64;
   bool timeKernels = false;
-  cudaEvent_t ev[kRing][3] = {};
+  cudaEvent_t ev[kRing][4] = {};  // start, partition end, end, partition start
+  int lastForm = turtle::kRuleAuto;  // form of the last enqueued sort
   long long timed = 0;
 };
 
@@ -127,7 +129,7 @@ turtle_status alloc_workspace(turtle_sorter* s, long long extraLeaves) {
     ts = p.tileShift < ts ? p.tileShift : ts;
     lc = p.leafCut < lc ? p.leafCut : lc;
   }
-  s->lay = make_layout(s->maxN, 1 << ts, lc, extraLeaves);
+  s->lay = make_layout(s->maxN, 1 << ts, lc, extraLeaves, true, s->width);
   TRY_CUDA(s, turtle::vmm_alloc(&s->ws, s->lay.bytes, s->device, false));
   return TURTLE_OK;
 }
@@ -145,6 +147,7 @@ turtle::SortArgs make_args(turtle_sorter* s, void* keys, int32_t* idx, const lon
   a.slices = slices;
   a.leafYield = s->leafYield;
   a.barrierPolls = s->barrierPolls;
+  a.radixStall = s->radixStall;
   return a;
 }
 
@@ -164,13 +167,18 @@ cudaError_t enqueue_persistent(turtle_sorter* s, const turtle::SortArgs& a, bool
   const int grid = full / (a.gridDiv > 0 ? a.gridDiv : 1);
   e = turtle::kernels_launch_persistent(s->width, hasIdx, a, grid > 0 ? grid : 1, st,
                                         timing ? ev[1] : nullptr,
-                                        a.slices > 1 ? s->sliceEv : nullptr);
+                                        a.slices > 1 ? s->sliceEv : nullptr,
+                                        timing ? ev[3] : nullptr);
   if (e != cudaSuccess) return e;
   if (timing) {
     if ((e = cudaEventRecord(ev[2], st)) != cudaSuccess) return e;
     ++s->timed;
   }
-  s->launches.fetch_add(1 + a.slices);  // partition + leaf launches
+  // partition + leaf launches, or the radix form's kernels
+  s->launches.fetch_add(a.radix ? turtle::radix_launches(s->width) : 1 + a.slices);
+  s->lastForm = a.radix ? turtle::kRuleRadix
+                        : a.samples == turtle::kWideSamples ? turtle::kRuleTwoLevel
+                        : a.samples == 3 ? turtle::kRuleReference : turtle::kRuleSampled;
   s->lastArgs = a;
   s->lastArgs.resume = 1;
   s->lastHasIdx = hasIdx;
@@ -570,6 +578,8 @@ int64_t turtle_launch_count(const turtle_sorter* s) { return s ? s->launches.loa
 
 int turtle_last_levels(const turtle_sorter* s) { return s ? s->lastLevels : 0; }
 
+int turtle_last_form(const turtle_sorter* s) { return s ? s->lastForm : -1; }
+
 int64_t turtle_max_elements(turtle_dtype dtype, int track_index) {
   (void)track_index;
   return dtype_width(dtype) ? kMaxElements : 0;
@@ -620,7 +630,7 @@ int turtle_debug_timeline(const turtle_sorter* s, uint64_t* ns, int32_t* info, i
 }
 
 turtle_status turtle_set_pivot_rule(turtle_sorter* s, int rule) {
-  if (!s || rule < turtle::kRuleReference || rule > turtle::kRuleAuto)
+  if (!s || rule < turtle::kRuleReference || rule > turtle::kRuleRadix)
     return TURTLE_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lk(s->mu);
   free_graphs(s);  // captured launches hold the old rule
@@ -660,6 +670,26 @@ int turtle_debug_kernel_times(turtle_sorter* s, int last, double* partition_ms, 
   return (int)n;
 }
 
+int turtle_debug_pass_times(turtle_sorter* s, int last, double* setup_ms, double* pass_ms) {
+  if (!s || !s->timeKernels || last <= 0) return 0;
+  const long long n = std::min<long long>(std::min<long long>(last, s->timed), turtle_sorter::kRing);
+  double su = 0, pm = 0;
+  for (long long k = s->timed - n; k < s->timed; ++k) {
+    cudaEvent_t* ev = s->ev[k % turtle_sorter::kRing];
+    float a = 0, b = 0;
+    if (cudaEventSynchronize(ev[2]) != cudaSuccess || cudaEventElapsedTime(&a, ev[0], ev[3]) != cudaSuccess ||
+        cudaEventElapsedTime(&b, ev[3], ev[1]) != cudaSuccess) {
+      cudaGetLastError();
+      return 0;
+    }
+    su += a;
+    pm += b;
+  }
+  if (setup_ms) *setup_ms = su;
+  if (pass_ms) *pass_ms = pm;
+  return (int)n;
+}
+
 int turtle_debug_error_site(const turtle_sorter* s, int* site, int* block, int* info) {
   if (!s || !s->hctrl) return 0;
   if (site) *site = s->hctrl->errSite;
@@ -684,6 +714,13 @@ turtle_status turtle_debug_barrier_polls(turtle_sorter* s, int64_t polls) {
   return TURTLE_OK;
 }
 
+turtle_status turtle_debug_radix_stall(turtle_sorter* s, int64_t tile) {
+  if (!s) return TURTLE_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->radixStall = tile < 0 ? 0 : tile + 1;
+  return TURTLE_OK;
+}
+
 turtle_status turtle_set_tuning(turtle_sorter* s, int enable) {
   if (!s) return TURTLE_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lk(s->mu);
@@ -701,7 +738,8 @@ turtle_status turtle_set_config(turtle_sorter* s, int form, int tile_shift, int 
     s->pinned = false;
     return TURTLE_OK;
   }
-  if ((form != turtle::kRuleSampled && form != turtle::kRuleTwoLevel) ||
+  if ((form != turtle::kRuleSampled && form != turtle::kRuleTwoLevel &&
+       form != turtle::kRuleRadix) ||
       tile_shift < turtle::kMinTileShift || tile_shift > turtle::kMaxTileShift ||
       leaf_geometry < 0 || leaf_geometry >= turtle::kLeafGeometries ||
       (grid_div != 1 && grid_div != 2 && grid_div != 4))
@@ -710,11 +748,13 @@ turtle_status turtle_set_config(turtle_sorter* s, int form, int tile_shift, int 
   turtle::kernels_leaf_geometry(s->width, leaf_geometry, nullptr, nullptr, &cap, nullptr);
   if (leaf_cut < turtle::kMinLeafCut || leaf_cut > cap) return TURTLE_ERR_INVALID_ARGUMENT;
   turtle::TuneParams p;
-  p.form = form;
+  p.form = form;  // TURTLE_FORM_RADIX: radix for plain sorts, two-level passes for batched ones
   p.tileShift = tile_shift;
   p.leafGeom = leaf_geometry;
   p.leafCut = leaf_cut;
   p.gridDiv = grid_div;
+  p.radix = 0;
+  p = turtle::tune_sanitize(s->width, p);
   const bool relayout = tile_shift < s->lay.tileShift || leaf_cut < s->lay.leafMax;
   s->pin = p;
   s->pinned = true;
@@ -727,15 +767,16 @@ turtle_status turtle_set_config(turtle_sorter* s, int form, int tile_shift, int 
 }
 
 turtle_status turtle_tuning_lookup(turtle_dtype dtype, int track_index, int64_t n,
-                                   int32_t* out5) {
+                                   int32_t* out6) {
   const int w = turtle::dtype_width(dtype);
-  if (!w || !out5 || n < 0) return TURTLE_ERR_INVALID_ARGUMENT;
+  if (!w || !out6 || n < 0) return TURTLE_ERR_INVALID_ARGUMENT;
   const turtle::TuneParams p = turtle::tune_lookup(w, track_index != 0, n);
-  out5[0] = p.form;
-  out5[1] = p.tileShift;
-  out5[2] = p.leafGeom;
-  out5[3] = p.leafCut;
-  out5[4] = p.gridDiv;
+  out6[0] = p.form;
+  out6[1] = p.tileShift;
+  out6[2] = p.leafGeom;
+  out6[3] = p.leafCut;
+  out6[4] = p.gridDiv;
+  out6[5] = p.radix;
   return TURTLE_OK;
 }
 

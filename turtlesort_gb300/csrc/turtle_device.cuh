@@ -182,6 +182,22 @@ struct Control {
   int tlInfo[kTimeline];             // work items of the phase that just ended
 };
 
+// ---- LSD radix form (turtle_radix.cu) ----
+// One pass per 8-bit digit; a pass CTA of kRadixThreads threads ranks a tile
+// of kRadixThreads x radix_items(width) keys.
+constexpr int kRadixThreads = 256;
+constexpr int kRadixBins = 256;
+constexpr long long kRadixMaxN = (1LL << 31) - 2;  // look-back words hold prefix + 1 in 31 bits
+__host__ __device__ constexpr int radix_items(int width) { return width == 8 ? 8 : 16; }
+__host__ __device__ constexpr int radix_tile(int width) { return kRadixThreads * radix_items(width); }
+
+struct RadixCtl {
+  int ord[8];            // rank of digit p among the digits that move keys (-1: skipped)
+  unsigned tileCtr[8];   // tile claim counter of digit p's pass
+  int active;            // digits that move keys
+  int last;              // the last of them (-1: none)
+};
+
 struct SortArgs {
   void* keysA;            // input and final output
   int* idxA;
@@ -219,6 +235,13 @@ struct SortArgs {
   int leafVariant;           // geometry of the leaf kernel (see kernels_leaf_geometry)
   int gridDiv;               // the partition kernel runs on (resident CTAs) / gridDiv CTAs
   Control* ctrl;
+  int radix;                 // 1: LSD radix form (radix kernels instead of partition + leaf)
+  int radixTiles;            // rows of each look-back region
+  unsigned* radixHist;       // [key bytes][256] digit counts
+  unsigned* radixBase;       // [key bytes][256] first output position of each digit
+  RadixCtl* radixCtl;
+  unsigned* radixStatus;     // [2][radixTiles][256] look-back words
+  long long radixStall;      // testing: tile + 1 whose look-back words are never published (0: none)
 };
 
 // ---- atomics / barrier ----
@@ -234,6 +257,7 @@ __device__ __forceinline__ int ld_acquire_int(int* p) {
 constexpr int kSiteBarrier = 1;    // grid_barrier spin limit
 constexpr int kSiteBulk = 3;       // bulk-copy barrier wait limit
 constexpr int kSiteCapacity = 4;   // a work list was full
+constexpr int kSiteLookback = 5;   // radix look-back poll limit
 
 __device__ __forceinline__ void set_error(Control* c, int code, int site = 0, int info = 0) {
   cuda::atomic_ref<int, cuda::thread_scope_device> a(c->error);

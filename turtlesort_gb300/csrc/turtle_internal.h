@@ -16,9 +16,20 @@ cudaError_t kernels_prepare(int width, bool hasIdx, int device, int* grid);
 // is not null it is recorded between the two launches.
 // Partition kernel, then a.slices leaf launches; sliceDone[s] (optional) is
 // recorded after leaf launch s, when every key below slice s's end is final.
+// passStart (optional) is recorded where the partition (or the radix form's
+// digit passes) begins.
 cudaError_t kernels_launch_persistent(int width, bool hasIdx, const SortArgs& a, int grid,
                                       cudaStream_t stream, cudaEvent_t mid = nullptr,
-                                      const cudaEvent_t* sliceDone = nullptr);
+                                      const cudaEvent_t* sliceDone = nullptr,
+                                      cudaEvent_t passStart = nullptr);
+// LSD radix form of a plain sort (a.radix == 1; turtle_radix.cu): histogram,
+// plan, one pass per key byte, finish.  Same events as the partition path;
+// every slice event is recorded at the end.
+cudaError_t kernels_launch_radix(int width, bool hasIdx, const SortArgs& a, cudaStream_t stream,
+                                 cudaEvent_t mid = nullptr, const cudaEvent_t* sliceDone = nullptr,
+                                 cudaEvent_t passStart = nullptr);
+// Kernel launches of one radix-form sort of `width`-byte keys.
+int radix_launches(int width);
 cudaError_t kernels_launch_multisort(int width, bool hasIdx, void* keys, int* idx,
                                      long long numArrays, int arrSize, unsigned long long flip,
                                      int fbits, int geometry, cudaStream_t stream);

@@ -24,12 +24,15 @@ struct WsLayout {
   size_t offCls = 0;
   int tileShift = 11;    // the smallest partition tile the lists are sized for
   int leafMax = 0;       // the smallest leaf cut the lists are sized for
+  int radixTiles = 0;    // look-back rows of the radix form (0: no radix form)
+  size_t offRadixHist = 0, offRadixBase = 0, offRadixCtl = 0, offRadixStatus = 0;
 };
 
 // classBytes: room for the per-key class bytes of two-level passes (without
-// it, sorts use one-level passes only).
+// it, sorts use one-level passes only).  radixWidth: key bytes of the radix
+// form's histograms and look-back words (0: no radix form).
 inline WsLayout make_layout(long long maxN, int tile, int leafMax, long long extraLeaves,
-                            bool classBytes = true) {
+                            bool classBytes = true, int radixWidth = 0) {
   WsLayout L;
   L.tileShift = 0;
   while ((1 << L.tileShift) < tile) ++L.tileShift;
@@ -62,6 +65,16 @@ inline WsLayout make_layout(long long maxN, int tile, int leafMax, long long ext
   L.offLeavesSorted = o; o = align_up(o + leafCap * sizeof(turtle::LeafDesc), 256);
   L.offFills = o; o = align_up(o + fillCap * sizeof(turtle::FillDesc), 256);
   if (classBytes) { L.hasCls = true; L.offCls = o; o = align_up(o + (size_t)maxN + 16, 256); }
+  if (radixWidth > 0) {
+    const long long rt = (maxN + radix_tile(radixWidth) - 1) / radix_tile(radixWidth);
+    L.radixTiles = (int)(rt > 0 ? rt : 1);
+    const size_t hb = (size_t)8 * kRadixBins * sizeof(unsigned);
+    L.offRadixHist = o; o = align_up(o + hb, 256);
+    L.offRadixBase = o; o = align_up(o + hb, 256);
+    L.offRadixCtl = o; o = align_up(o + sizeof(RadixCtl), 256);
+    L.offRadixStatus = o;
+    o = align_up(o + (size_t)2 * L.radixTiles * kRadixBins * sizeof(unsigned), 256);
+  }
   L.bytes = o;
   return L;
 }
@@ -103,6 +116,7 @@ constexpr int kRuleReference = 0;
 constexpr int kRuleSampled = 1;
 constexpr int kRuleTwoLevel = 2;
 constexpr int kRuleAuto = 3;                      // two-level from kAutoTwoLevelKeys keys up
+constexpr int kRuleRadix = 4;                     // LSD radix passes (plain sorts)
 constexpr long long kAutoTwoLevelKeys = 1LL << 23;  // measured crossover on GB300
 inline int rule_samples(int rule) {
   return rule == kRuleReference ? 3 : rule == kRuleTwoLevel ? kWideSamples : kSamples;
@@ -153,8 +167,21 @@ inline SortArgs bind_args(void* keys, int* idx, void* keysB, int* idxB, char* ws
   }
   if (tp.leafCut < L.leafMax) tp.leafCut = L.leafMax < cap ? L.leafMax : cap;
   if (tp.tileShift < L.tileShift) tp.tileShift = L.tileShift;
-  if (rule == kRuleAuto) rule = tp.form;
+  if (rule == kRuleAuto) rule = tp.radix ? kRuleRadix : tp.form;
+  if (rule == kRuleRadix) {
+    // one array whose tiles fit the look-back rows; otherwise the pivot form
+    const long long rt = (n + radix_tile(width) - 1) / radix_tile(width);
+    if (offs == nullptr && L.radixTiles > 0 && rt <= L.radixTiles && n <= kRadixMaxN) a.radix = 1;
+    rule = tp.form;
+  }
   if (rule == kRuleTwoLevel && !L.hasCls) rule = kRuleSampled;
+  if (L.radixTiles > 0) {
+    a.radixTiles = L.radixTiles;
+    a.radixHist = (unsigned*)(ws + L.offRadixHist);
+    a.radixBase = (unsigned*)(ws + L.offRadixBase);
+    a.radixCtl = (RadixCtl*)(ws + L.offRadixCtl);
+    a.radixStatus = (unsigned*)(ws + L.offRadixStatus);
+  }
   a.cls = L.hasCls ? (unsigned char*)(ws + L.offCls) : nullptr;
   a.samples = rule_samples(rule);
   a.slices = 1;

@@ -1,0 +1,448 @@
+// LSD radix form of the plain sort (TURTLE_FORM_RADIX).
+//
+// The reference sorts by 3-pivot partitioning (turtle-sort.cu:573-934) and
+// its output is the stable order of the keys (ids of equal keys in input
+// order), which every stable sort produces.  This form reaches the same bytes
+// in passes over 8-bit digits, least significant first; each pass is a stable
+// counting scatter, so the composition is the stable sort:
+//
+//   radix_hist_kernel    one read of the keys: the 256-bin histogram of every
+//                        digit at once (float keys are mapped to their
+//                        totalOrder images here, in place);
+//   radix_plan_kernel    one CTA: the first output position of each digit
+//                        value (exclusive prefix of each histogram); a digit
+//                        whose keys all share one value is skipped, its
+//                        scatter would be the identity;
+//   radix_pass_kernel    one launch per digit, one CTA per tile of
+//                        kRadixThreads x radix_items keys, tiles claimed in
+//                        order with an atomic counter.  The CTA counts its
+//                        keys' digit values and publishes the counts, adds the
+//                        counts of the tiles before it by a decoupled
+//                        look-back over their published words, ranks its keys
+//                        by digit (per-warp running counts; the lanes of one
+//                        digit value found with shared-memory atomicOr, which
+//                        measured 2.5x faster than a match instruction on
+//                        ~30 distinct values per warp), stages the tile in
+//                        shared memory in digit order and writes it out,
+//                        consecutive keys of a digit to consecutive addresses;
+//   radix_finish_kernel  the result back into the caller's buffer when an odd
+//                        number of passes left it in the scratch buffer (and
+//                        float keys back from their images when no pass ran).
+//
+// Every pass reads keys + ids once and writes them once; the histogram pass
+// reads the keys once more.  A look-back wait is bounded: past the poll limit
+// the CTA records kDevTimeout, publishes its word (so later tiles go on) and
+// writes nothing.
+#include <cuda_runtime.h>
+
+#include <cuda/atomic>
+
+#include "turtle_device.cuh"
+#include "turtle_internal.h"
+
+namespace turtle {
+namespace {
+
+constexpr unsigned kRFull = 0xffffffffu;
+constexpr unsigned kLbInclusive = 0x80000000u;  // word holds the inclusive prefix, else the tile's count
+constexpr int kRWarps = kRadixThreads / 32;
+static_assert(kRadixThreads == kRadixBins, "one pass thread per digit value");
+
+// Look-back words: 0 = not published; else flag | (value + 1).
+__device__ __forceinline__ unsigned lb_load(const unsigned* p) {
+  cuda::atomic_ref<const unsigned, cuda::thread_scope_device> a(*p);
+  return a.load(cuda::memory_order_relaxed);
+}
+__device__ __forceinline__ void lb_store(unsigned* p, unsigned v) {
+  cuda::atomic_ref<unsigned, cuda::thread_scope_device> a(*p);
+  a.store(v, cuda::memory_order_relaxed);
+}
+
+// totalOrder image of an IEEE-754 bit pattern (forward), or back (inverse).
+template <typename U>
+__device__ __forceinline__ U float_image(U b, bool inverse) {
+  constexpr U kSign = U(1) << (8 * sizeof(U) - 1);
+  const bool top = (b & kSign) != 0;
+  const U mask = (top != inverse) ? U(~U(0)) : kSign;
+  return b ^ mask;
+}
+
+template <typename U>
+__global__ void __launch_bounds__(kRadixThreads) radix_hist_kernel(SortArgs a) {
+  using KT = typename KeyCfg<U>::KT;
+  constexpr int P = sizeof(U);
+  __shared__ unsigned h[P * kRadixBins];
+  const int tid = threadIdx.x, lane = tid & 31;
+  for (int i = tid; i < P * kRadixBins; i += kRadixThreads) h[i] = 0u;
+  // the first moving pass uses look-back region 0: clear its rows
+  {
+    const long long rows = (a.n + radix_tile(P) - 1) / radix_tile(P);
+    const long long words = rows * kRadixBins;
+    for (long long i = (long long)blockIdx.x * kRadixThreads + tid; i < words;
+         i += (long long)gridDim.x * kRadixThreads)
+      a.radixStatus[i] = 0u;
+  }
+  __syncthreads();
+  U* keys = (U*)a.keysA;
+  const long long n = a.n;
+  const KT flip = (KT)a.flip;
+  const bool fl = sizeof(U) >= 4 && a.fbits != 0;
+  const long long step = (long long)gridDim.x * kRadixThreads * 4;
+  // a warp takes 128 consecutive keys per round (four coalesced loads)
+  for (long long base = ((long long)blockIdx.x * kRadixThreads + (tid & ~31)) * 4; base < n;
+       base += step) {
+    KT k[4];
+    bool ok[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const long long e = base + 32 * q + lane;
+      ok[q] = e < n;
+      U raw = ok[q] ? keys[e] : U(0);
+      if (fl && ok[q]) {
+        raw = float_image<U>(raw, false);
+        keys[e] = raw;
+      }
+      k[q] = KT(raw) ^ flip;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        const unsigned d = (unsigned)(k[q] >> (8 * p)) & 255u;
+        const unsigned d0 = __shfl_sync(kRFull, d, 0);
+        // sorted and narrow inputs give whole warps of one digit value
+        if (__all_sync(kRFull, ok[q] && d == d0)) {
+          if (lane == 0) atomicAdd(&h[p * kRadixBins + d], 32u);
+        } else if (ok[q]) {
+          atomicAdd(&h[p * kRadixBins + d], 1u);
+        }
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = tid; i < P * kRadixBins; i += kRadixThreads)
+    if (h[i] != 0u) atomicAdd(&a.radixHist[i], h[i]);
+}
+
+template <typename U>
+__global__ void __launch_bounds__(kRadixBins) radix_plan_kernel(SortArgs a) {
+  constexpr int P = sizeof(U);
+  const int b = threadIdx.x, lane = b & 31, warp = b >> 5;
+  __shared__ unsigned wsum[kRadixBins / 32];
+  RadixCtl* c = a.radixCtl;
+  int ord = 0, last = -1;
+  for (int p = 0; p < P; ++p) {
+    const unsigned cnt = a.radixHist[p * kRadixBins + b];
+    const int skip = __syncthreads_or(cnt == (unsigned)a.n);
+    unsigned x = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(kRFull, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    unsigned pre = 0;
+    for (int w = 0; w < warp; ++w) pre += wsum[w];
+    a.radixBase[p * kRadixBins + b] = pre + x - cnt;
+    __syncthreads();
+    if (b == 0) {
+      c->ord[p] = skip ? -1 : ord;
+      c->tileCtr[p] = 0u;
+    }
+    if (!skip) {
+      last = p;
+      ++ord;
+    }
+  }
+  if (b == 0) {
+    for (int p = P; p < 8; ++p) c->ord[p] = -1;
+    c->active = ord;
+    c->last = last;
+    a.ctrl->levels = ord;
+  }
+}
+
+// One pass over digit p (bits 8p .. 8p+7 of the unsigned key image).  With
+// ids a thread holds 2 x kItems loaded words: three resident CTAs per SM
+// leave it enough registers.
+//
+// Order of work in a tile: load; count the tile's digit values (shared
+// atomics) and publish the counts at once, so later tiles can add them; rank
+// and scan (no other tile needed); look back and publish the inclusive prefix;
+// stage and write.  Measured on 2^26 int32 keys + ids: 1.88 ms in this order,
+// 1.99 ms when the look-back runs before the ranking (with or without its
+// first loads issued early), 2.53 ms when the counts are published only after
+// the ranking.
+template <typename U, bool kIdx>
+__global__ void __launch_bounds__(kRadixThreads, kIdx ? 3 : 4) radix_pass_kernel(SortArgs a, int p) {
+  using KT = typename KeyCfg<U>::KT;
+  constexpr int kItems = radix_items(sizeof(U));
+  constexpr int kTile = kRadixThreads * kItems;
+  static_assert(kTile <= 65535, "per-warp counts and offsets are 16-bit");
+  __shared__ int s_tile;
+  __shared__ int s_fail;
+  __shared__ unsigned short s_wc[kRWarps][kRadixBins];  // warp running counts, then warp offsets
+  __shared__ unsigned s_mm[kRWarps][kRadixBins];        // lanes of each digit value (one item)
+  __shared__ unsigned s_cnt[kRadixBins];                // the tile's count of each digit value
+  __shared__ int s_start[kRadixBins];                   // first staging slot of each digit value
+  __shared__ int s_dst[kRadixBins];                     // output position of staging slot 0, per value
+  __shared__ unsigned s_wsum[kRWarps];
+  __shared__ U s_k[kTile];
+  __shared__ int s_i[kIdx ? kTile : 1];
+
+  const RadixCtl* c = a.radixCtl;
+  const int ord = c->ord[p];
+  if (ord < 0) return;  // every key has the same digit: nothing moves
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const bool lastPass = p == c->last;
+  const bool fromB = (ord & 1) != 0;
+  const U* srcK = (const U*)(fromB ? a.keysB : a.keysA);
+  U* dstK = (U*)(fromB ? a.keysA : a.keysB);
+  const int* srcI = fromB ? a.idxB : a.idxA;
+  int* dstI = fromB ? a.idxA : a.idxB;
+  const long long n = a.n;
+  const long long tiles = (n + kTile - 1) / kTile;
+  unsigned* own = a.radixStatus + (size_t)(ord & 1) * a.radixTiles * kRadixBins;
+  unsigned* other = a.radixStatus + (size_t)((ord & 1) ^ 1) * a.radixTiles * kRadixBins;
+
+  if (tid == 0) {
+    s_tile = (int)atomicAdd(&a.radixCtl->tileCtr[p], 1u);
+    s_fail = 0;
+  }
+  for (int i = lane; i < kRadixBins; i += 32) {
+    s_wc[warp][i] = 0;
+    s_mm[warp][i] = 0u;
+  }
+  s_cnt[tid] = 0u;
+  __syncthreads();
+  const int tile = s_tile;
+  if (tile >= tiles) return;  // the grid is exactly `tiles` CTAs
+  const int b = tid;  // the digit value this thread counts, scans and looks back for
+  const unsigned gbase = a.radixBase[p * kRadixBins + b];
+  // the next moving pass uses the other region: clear this tile's row of it
+  // (the pass that used it last has finished)
+  other[(size_t)tile * kRadixBins + tid] = 0u;
+
+  const KT flip = (KT)a.flip;
+  const int shift = 8 * p;
+  // warp-striped items: item i of this lane is tile element w*32*kItems + 32i + lane
+  const long long e0 = (long long)tile * kTile + (long long)warp * 32 * kItems + lane;
+  KT key[kItems];
+  int id[kIdx ? kItems : 1];
+#pragma unroll
+  for (int i = 0; i < kItems; ++i) {
+    const long long e = e0 + 32 * i;
+    const bool ok = e < n;
+    key[i] = ok ? KT(__ldcs(srcK + e)) ^ flip : KT(0);
+    if (kIdx) id[i] = ok ? __ldcs(srcI + e) : 0;
+  }
+  // 1. the tile's digit counts, published at once
+#pragma unroll
+  for (int i = 0; i < kItems; ++i)
+    if (e0 + 32 * i < n) atomicAdd(&s_cnt[(unsigned)(key[i] >> shift) & 255u], 1u);
+  __syncthreads();
+  const unsigned cnt = s_cnt[b];
+  unsigned* row = own + (size_t)tile * kRadixBins;
+  const bool mute = a.radixStall == (long long)tile + 1;  // testing: later tiles wait in vain
+  if (!mute) lb_store(&row[b], (tile == 0 ? kLbInclusive : 0u) | (cnt + 1u));
+  // 2. rank: item by item in memory order (stable).  The lanes of one digit
+  // value are found by each setting its bit in the warp's word for that value;
+  // the warp's running count of the value is updated by the group's highest lane.
+  unsigned lt;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+  unsigned rk[kItems / 2];
+  unsigned short* wc = s_wc[warp];
+  unsigned* mm = s_mm[warp];
+#pragma unroll
+  for (int i = 0; i < kItems; ++i) {
+    const bool ok = e0 + 32 * i < n;
+    const unsigned d = (unsigned)(key[i] >> shift) & 255u;
+    if (ok) atomicOr(&mm[d], 1u << lane);
+    __syncwarp();
+    const unsigned peers = ok ? mm[d] : 0u;
+    unsigned base = 0, r = 0;
+    if (ok) {
+      base = wc[d];
+      r = base + __popc(peers & lt);
+    }
+    __syncwarp();
+    if (ok && (peers >> lane) == 1u) {
+      wc[d] = (unsigned short)(base + __popc(peers));
+      mm[d] = 0u;
+    }
+    __syncwarp();
+    if (i & 1) rk[i >> 1] |= r << 16;
+    else rk[i >> 1] = r;
+  }
+  __syncthreads();
+  // 3. warp offsets of digit value b, and its first staging slot (exclusive
+  // prefix of the tile's counts over the digit values)
+  {
+    unsigned run = 0;
+#pragma unroll
+    for (int w = 0; w < kRWarps; ++w) {
+      const unsigned x = s_wc[w][b];
+      s_wc[w][b] = (unsigned short)run;
+      run += x;
+    }
+    unsigned x = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(kRFull, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) s_wsum[warp] = x;
+    __syncthreads();
+    unsigned pre = 0;
+#pragma unroll
+    for (int w = 0; w < kRWarps; ++w) pre += w < warp ? s_wsum[w] : 0u;
+    s_start[b] = (int)(pre + x - cnt);
+  }
+  // 4. decoupled look-back: add the published words of the tiles before this
+  // one, four at a time, back to the first inclusive prefix
+  unsigned excl = 0;
+  if (tile > 0) {
+    const long long limit = a.barrierPolls > 0 ? a.barrierPolls : kSpinLimit;
+    long long polls = 0;
+    long long j = tile - 1;
+    for (;;) {
+      unsigned w[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        w[q] = j - q >= 0 ? lb_load(own + (size_t)(j - q) * kRadixBins + b) : (kLbInclusive | 1u);
+      bool stop = false, incl = false;
+      int used = 0;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (!stop) {
+          if (w[q] == 0u) {
+            stop = true;  // not published yet: poll it again
+          } else {
+            excl += (w[q] & ~kLbInclusive) - 1u;
+            ++used;
+            if (w[q] & kLbInclusive) incl = stop = true;
+          }
+        }
+      }
+      if (incl) break;
+      j -= used;
+      if (used == 0 &&
+          (++polls > limit || ((polls & 255) == 0 && ld_acquire_int(&a.ctrl->error) != 0))) {
+        set_error(a.ctrl, kDevTimeout, kSiteLookback, tile);
+        s_fail = 1;
+        break;
+      }
+    }
+    if (!mute) lb_store(&row[b], kLbInclusive | (excl + cnt + 1u));
+  }
+  s_dst[b] = (int)(gbase + excl) - s_start[b];
+  __syncthreads();
+  // 5. stage the tile in digit order
+#pragma unroll
+  for (int i = 0; i < kItems; ++i) {
+    if (e0 + 32 * i < n) {
+      const unsigned d = (unsigned)(key[i] >> shift) & 255u;
+      const unsigned r = (i & 1) ? rk[i >> 1] >> 16 : rk[i >> 1] & 0xFFFFu;
+      const int pos = s_start[d] + (int)s_wc[warp][d] + (int)r;
+      s_k[pos] = U(key[i] ^ flip);
+      if (kIdx) s_i[pos] = id[i];
+    }
+  }
+  __syncthreads();
+  if (s_fail) return;
+  // 6. write-out: thread t takes staging slots t, t + 256, ...; consecutive
+  // slots of one digit value go to consecutive addresses
+  const long long left = n - (long long)tile * kTile;
+  const int valid = left < kTile ? (int)left : kTile;
+#pragma unroll
+  for (int i = 0; i < kItems; ++i) {
+    const int s = i * kRadixThreads + tid;
+    if (s < valid) {
+      U raw = s_k[s];
+      const unsigned d = (unsigned)((KT(raw) ^ flip) >> shift) & 255u;
+      const long long dst = (long long)s_dst[d] + s;
+      if (dst >= 0 && dst < n) {  // always, when the look-back completed
+        if (sizeof(U) >= 4 && lastPass && a.fbits != 0) raw = float_image<U>(raw, true);
+        dstK[dst] = raw;
+        if (kIdx) dstI[dst] = s_i[s];
+      }
+    }
+  }
+}
+
+template <typename U, bool kIdx>
+__global__ void __launch_bounds__(256) radix_finish_kernel(SortArgs a) {
+  const int active = a.radixCtl->active;
+  const bool inB = (active & 1) != 0;
+  const bool unmap = sizeof(U) >= 4 && active == 0 && a.fbits != 0;
+  if (!inB && !unmap) return;
+  U* ka = (U*)a.keysA;
+  const U* kb = (const U*)a.keysB;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+    if (inB) {
+      ka[i] = kb[i];  // the last pass already mapped float images back
+      if (kIdx) a.idxA[i] = a.idxB[i];
+    } else {
+      ka[i] = float_image<U>(ka[i], true);
+    }
+  }
+}
+
+int device_sms() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms > 0 ? sms : 1;
+}
+
+template <typename U, bool kIdx>
+cudaError_t launch_radix(const SortArgs& a, cudaStream_t stream, cudaEvent_t mid,
+                         const cudaEvent_t* sliceDone, cudaEvent_t passStart) {
+  constexpr int P = sizeof(U);
+  const long long tiles = (a.n + radix_tile(P) - 1) / radix_tile(P);
+  if (a.n < 2) return cudaSuccess;
+  if (tiles > a.radixTiles || a.radixHist == nullptr) return cudaErrorInvalidValue;
+  const int sms = device_sms();
+  cudaError_t e = cudaMemsetAsync(a.radixHist, 0, (size_t)P * kRadixBins * sizeof(unsigned), stream);
+  if (e != cudaSuccess) return e;
+  const long long hb = (a.n + 4LL * kRadixThreads - 1) / (4LL * kRadixThreads);
+  const long long histBlocks = hb < 8LL * sms ? hb : 8LL * sms;
+  radix_hist_kernel<U><<<(unsigned)(histBlocks > 0 ? histBlocks : 1), kRadixThreads, 0, stream>>>(a);
+  radix_plan_kernel<U><<<1, kRadixBins, 0, stream>>>(a);
+  if (passStart != nullptr && (e = cudaEventRecord(passStart, stream)) != cudaSuccess) return e;
+  for (int p = 0; p < P; ++p) radix_pass_kernel<U, kIdx><<<(unsigned)tiles, kRadixThreads, 0, stream>>>(a, p);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (mid != nullptr && (e = cudaEventRecord(mid, stream)) != cudaSuccess) return e;
+  const long long fb = (a.n + 255) / 256;
+  radix_finish_kernel<U, kIdx><<<(unsigned)(fb < 8LL * sms ? fb : 8LL * sms), 256, 0, stream>>>(a);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  // every key is final only now: all result slices complete together
+  if (sliceDone != nullptr)
+    for (int sl = 0; sl < a.slices; ++sl)
+      if ((e = cudaEventRecord(sliceDone[sl], stream)) != cudaSuccess) return e;
+  return cudaSuccess;
+}
+
+}  // namespace
+
+int radix_launches(int width) { return width + 3; }
+
+cudaError_t kernels_launch_radix(int width, bool hasIdx, const SortArgs& a, cudaStream_t stream,
+                                 cudaEvent_t mid, const cudaEvent_t* sliceDone,
+                                 cudaEvent_t passStart) {
+  switch (width) {
+    case 1: return hasIdx ? launch_radix<uint8_t, true>(a, stream, mid, sliceDone, passStart)
+                          : launch_radix<uint8_t, false>(a, stream, mid, sliceDone, passStart);
+    case 2: return hasIdx ? launch_radix<uint16_t, true>(a, stream, mid, sliceDone, passStart)
+                          : launch_radix<uint16_t, false>(a, stream, mid, sliceDone, passStart);
+    case 4: return hasIdx ? launch_radix<uint32_t, true>(a, stream, mid, sliceDone, passStart)
+                          : launch_radix<uint32_t, false>(a, stream, mid, sliceDone, passStart);
+    case 8: return hasIdx ? launch_radix<uint64_t, true>(a, stream, mid, sliceDone, passStart)
+                          : launch_radix<uint64_t, false>(a, stream, mid, sliceDone, passStart);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace turtle

@@ -112,7 +112,9 @@ namespace {
 size_t batch_bytes(int width, bool hasIdx, long long total, long long num, turtle::WsLayout* layOut) {
   int ts = 0, lc = 0;  // laid out for the configuration the table gives this batch
   turtle::tune_layout_bounds(width, hasIdx, std::max(total, 2LL), &ts, &lc);
-  const turtle::WsLayout lay = turtle::make_layout(std::max(total, 2LL), 1 << ts, lc, num);
+  // a batch of one request is a plain sort: room for the radix form too
+  const turtle::WsLayout lay = turtle::make_layout(std::max(total, 2LL), 1 << ts, lc, num, true,
+                                                   num == 1 ? width : 0);
   size_t b = 0;
   const size_t kb = turtle::align_up((size_t)total * width + 16, 256);
   const size_t ib = hasIdx ? turtle::align_up((size_t)total * 4 + 16, 256) : 0;
@@ -173,8 +175,9 @@ turtle_status launch_batch(turtle_server* s, Batch* b) {
                   s->sIn);
   cudaEventRecord(sl.inDone, s->sIn);
   // sort
-  b->args = turtle::bind_args(keys, idx, keysB, idxB, ws, b->lay, offs, num, b->total,
-                              b->dtype, turtle::kRuleAuto,
+  // one request: a plain sort (the tuned form, radix included); else batched
+  b->args = turtle::bind_args(keys, idx, keysB, idxB, ws, b->lay, num == 1 ? nullptr : offs,
+                              num == 1 ? 0 : num, b->total, b->dtype, turtle::kRuleAuto,
                               turtle::tune_lookup(b->width, b->hasIdx, b->total));
   cudaStream_t ss = s->sSort[b->slot % kSortStreams];
   cudaStreamWaitEvent(ss, sl.inDone, 0);

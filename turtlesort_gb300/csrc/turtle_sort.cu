@@ -1790,7 +1790,12 @@ cudaError_t kernels_prepare(int width, bool hasIdx, int device, int* grid) {
 
 cudaError_t kernels_launch_persistent(int width, bool hasIdx, const SortArgs& a, int grid,
                                       cudaStream_t stream, cudaEvent_t mid,
-                                      const cudaEvent_t* sliceDone) {
+                                      const cudaEvent_t* sliceDone, cudaEvent_t passStart) {
+  if (a.radix) return kernels_launch_radix(width, hasIdx, a, stream, mid, sliceDone, passStart);
+  if (passStart != nullptr) {
+    const cudaError_t e = cudaEventRecord(passStart, stream);
+    if (e != cudaSuccess) return e;
+  }
   TURTLE_WIDTH_DISPATCH(width, hasIdx,
                         (launch_persistent<U, I>(a, grid, stream, mid, sliceDone)));
 }

@@ -20,12 +20,18 @@ TuneParams tune_defaults(int width, long long n) {
   kernels_leaf_geometry(width, p.leafGeom, nullptr, nullptr, &cap, nullptr);
   p.leafCut = cap;
   p.gridDiv = 1;
+  p.radix = 0;
   return p;
 }
 
 TuneParams tune_sanitize(int width, TuneParams p) {
+  if (p.form == kRuleRadix) {  // radix for plain sorts, two-level passes for batched ones
+    p.form = kRuleTwoLevel;
+    p.radix = 1;
+  }
   if (p.form != kRuleSampled && p.form != kRuleTwoLevel && p.form != kRuleReference)
     p.form = kRuleSampled;
+  p.radix = p.radix != 0 ? 1 : 0;
   if (p.tileShift < kMinTileShift) p.tileShift = kMinTileShift;
   if (p.tileShift > kMaxTileShift) p.tileShift = kMaxTileShift;
   if (p.leafGeom < 0 || p.leafGeom >= kLeafGeometries) p.leafGeom = kDefaultLeafGeometry;

@@ -13,6 +13,8 @@
 //   leafCut    segments of at most leafCut keys go to the shared-memory sort
 //              (at most the geometry's capacity)
 //   gridDiv    the partition kernel runs on (resident CTAs) / gridDiv CTAs
+//   radix      1: plain (one-array) sorts use the LSD radix form instead; the
+//              pivot values above still configure batched sorts
 #pragma once
 
 #include <cstdint>
@@ -25,6 +27,7 @@ struct TuneParams {
   int leafGeom;
   int leafCut;
   int gridDiv;
+  int radix;
 };
 
 struct TuneEntry {  // plain and batched sorts: n (total keys) up to maxN
@@ -46,7 +49,7 @@ constexpr int kMinLeafCut = 1024;
 
 // Compile-time defaults (the configuration before tuning): two-level passes
 // from 2^23 keys, 2048-key tiles, 512 x 16 (512 x 8 for 64-bit keys) leaf
-// geometry at full capacity, every resident CTA.
+// geometry at full capacity, every resident CTA, no radix form.
 TuneParams tune_defaults(int width, long long n);
 // Table entry for (width, ids, n), else the defaults.
 TuneParams tune_lookup(int width, bool ids, long long n);

@@ -11,8 +11,10 @@ every combination of
   leaf cut   the geometry's capacity, or half of it
   grid       every resident partition CTA, or half of them (small sorts)
 
-and, per width x index flag x MultiSort array length, every shared-memory
-geometry that holds the arrays.  It writes
+then times the LSD radix form at the same size: the entry's radix flag is set
+when it beats the best pivot configuration (plain sorts then use it; batched
+sorts keep the pivot configuration).  Per width x index flag x MultiSort array
+length it times every shared-memory geometry that holds the arrays.  It writes
 
   turtlesort_gb300/csrc/turtle_tuning_table.inc   the table compiled into the
                                                   library (rebuild to use it)
@@ -20,6 +22,8 @@ geometry that holds the arrays.  It writes
                                                   winner and the default time
 
     python -m turtlesort_gb300.tune --out <dir> [--quick]
+    python -m turtlesort_gb300.tune --out <dir> --radix-only   # keep the pivot
+        configurations of the compiled table, re-measure only the radix flags
 
 The reference has no tuner: its geometry is fixed at compile time
 (turtle-sort.cu:7,12; turtle-multi-sort.cuh:11,13).
@@ -31,6 +35,7 @@ import ctypes as C
 import datetime
 import itertools
 import json
+import re
 import statistics
 import sys
 from pathlib import Path
@@ -44,7 +49,7 @@ import turtlesort_gb300 as ts  # noqa: E402
 from turtlesort_gb300 import datagen as dg  # noqa: E402
 
 TABLE = HERE / "csrc" / "turtle_tuning_table.inc"
-SAMPLED, TWO_LEVEL = 1, 2
+SAMPLED, TWO_LEVEL, RADIX = 1, 2, 4
 COMBOS = [(np.uint8, False), (np.uint8, True), (np.uint16, False), (np.uint16, True),
           (np.uint32, False), (np.uint32, True), (np.uint64, False), (np.uint64, True)]
 
@@ -131,18 +136,57 @@ def tune_sorts(torch, lib, bands, quick, reps, log):
                 ms = tm.run(cfg)
                 if ms is not None:
                     results.append((ms, cfg))
-            tm.close()
             results.sort()
             best_ms, best = results[0]
+            radix_ms = tm.run(radix_config(lib, dtype))
+            tm.close()
             row = {"width": np.dtype(dtype).itemsize, "ids": int(ids), "n": n,
-                   "default_ms": default, "best_ms": best_ms,
-                   "best": dict(zip(("form", "tile_shift", "geometry", "leaf_cut", "grid_div"), best)),
-                   "tried": len(results),
+                   "default_ms": default, "best_ms": best_ms, "radix_ms": radix_ms,
+                   "best": dict(zip(("form", "tile_shift", "geometry", "leaf_cut", "grid_div"), best),
+                                radix=int(radix_ms < best_ms)),
+                   "tried": len(results) + 1,
                    "top5": [{"ms": m, "cfg": list(c)} for m, c in results[:5]]}
             rows.append(row)
             log(f"w{row['width']} ids{ids} n={n}: default {default:.3f} ms, best {best_ms:.3f} ms "
-                f"{row['best']}")
+                f"{row['best']}, radix {radix_ms:.3f} ms")
     return rows
+
+
+def radix_config(lib, dtype):
+    """set_config arguments of the radix form (the other values are unused by
+    plain sorts)."""
+    return (RADIX, 11, 1, geometry(lib, dtype, 1)["capacity"], 1)
+
+
+def read_table():
+    """Sort and MultiSort entries of the compiled table."""
+    text = TABLE.read_text()
+    sorts = [tuple(int(x) for x in m.groups()) for m in re.finditer(
+        r"\{(\d+), (\d+), (\d+)LL, \{(\d+), (\d+), (\d+), (\d+), (\d+), (\d+)\}\}", text)]
+    multi = [tuple(int(x) for x in m.groups()) for m in re.finditer(
+        r"^\s+\{(\d+), (\d+), (\d+), (\d+)\},$", text, re.M)]
+    src = re.search(r'kTuneSourceText\[\] = "([^"]*)"', text).group(1)
+    return sorts, multi, src
+
+
+def tune_radix_flags(torch, lib, reps, log):
+    """The compiled table's pivot configurations, each timed against the radix
+    form at its band size; returns the rows with their radix flags."""
+    sorts, multi, src = read_table()
+    dtypes = {1: np.uint8, 2: np.uint16, 4: np.uint32, 8: np.uint64}
+    rows = []
+    for w, ids, max_n, form, tile, g, cut, gd, _ in sorts:
+        dtype = dtypes[w]
+        tm = Timer(torch, dtype, max_n, bool(ids), reps)
+        best_ms = tm.run((form, tile, g, cut, gd))
+        radix_ms = tm.run(radix_config(lib, dtype))
+        tm.close()
+        rows.append({"width": w, "ids": ids, "n": max_n, "best_ms": best_ms, "radix_ms": radix_ms,
+                     "best": {"form": form, "tile_shift": tile, "geometry": g, "leaf_cut": cut,
+                              "grid_div": gd, "radix": int(radix_ms < best_ms)}})
+        log(f"w{w} ids{ids} n={max_n}: pivot {best_ms:.3f} ms, radix {radix_ms:.3f} ms")
+    multi_rows = [{"width": w, "ids": i, "arr": a, "best": g} for w, i, a, g in multi]
+    return rows, multi_rows, src
 
 
 def tune_multisort(torch, lib, lens, reps, log):
@@ -197,7 +241,7 @@ def write_table(sort_rows, multi_rows, source):
     for r in sorted(sort_rows, key=lambda r: (r["width"], r["ids"], r["n"])):
         b = r["best"]
         lines.append(f"    {{{r['width']}, {r['ids']}, {r['n']}LL, {{{b['form']}, {b['tile_shift']}, "
-                     f"{b['geometry']}, {b['leaf_cut']}, {b['grid_div']}}}}},")
+                     f"{b['geometry']}, {b['leaf_cut']}, {b['grid_div']}, {b.get('radix', 0)}}}}},")
     lines += ["};", "static const turtle::MultiEntry kMultiTable[] = {"]
     for r in sorted(multi_rows, key=lambda r: (r["width"], r["ids"], r["arr"])):
         lines.append(f"    {{{r['width']}, {r['ids']}, {r['arr']}, {r['best']}}},")
@@ -211,6 +255,8 @@ def main() -> int:
     ap.add_argument("--quick", action="store_true", help="fewer tiles, full leaf cuts only")
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--max-log2", type=int, default=26)
+    ap.add_argument("--radix-only", action="store_true",
+                    help="re-measure only the radix flags of the compiled table")
     args = ap.parse_args()
     import torch
     out = Path(args.out)
@@ -222,12 +268,16 @@ def main() -> int:
         print(msg, flush=True)
         logf.write(msg + "\n")
 
-    bands = [1 << k for k in range(16, args.max_log2 + 1, 2)]
-    sort_rows = tune_sorts(torch, lib, bands, args.quick, args.reps, log)
-    multi_rows = tune_multisort(torch, lib, [16, 64, 256, 1024, 2048, 4096, 8192], args.reps, log)
     name = torch.cuda.get_device_name(0)
     when = datetime.datetime.now(datetime.timezone.utc).strftime("%Y-%m-%d")
-    source = f"tune.py on {name}, {when}, uniform keys, {len(sort_rows)} bands"
+    if args.radix_only:
+        sort_rows, multi_rows, old = tune_radix_flags(torch, lib, args.reps, log)
+        source = f"{old.split('; radix flags')[0]}; radix flags {when}"
+    else:
+        bands = [1 << k for k in range(16, args.max_log2 + 1, 2)]
+        sort_rows = tune_sorts(torch, lib, bands, args.quick, args.reps, log)
+        multi_rows = tune_multisort(torch, lib, [16, 64, 256, 1024, 2048, 4096, 8192], args.reps, log)
+        source = f"tune.py on {name}, {when}, uniform keys, {len(sort_rows)} bands"
     write_table(sort_rows, multi_rows, source)
     (out / "tuning.json").write_text(json.dumps({"source": source, "sorts": sort_rows,
                                                  "multisort": multi_rows}, indent=1))
