@@ -184,7 +184,10 @@ struct Control {
 
 // ---- LSD radix form (turtle_radix.cu) ----
 // One pass per 8-bit digit; a pass CTA of kRadixThreads threads ranks a tile
-// of kRadixThreads x radix_items(width) keys.
+// of kRadixThreads x radix_items(width) keys (4096, or 2048 for 64-bit keys).
+// Measured on 2^26 int32 keys + ids: 1.76 ms with 256 x 16, 2.12 ms with
+// 512 x 8 (more resident warps, but longer CTA barriers and half the threads
+// idle in the per-digit steps).
 constexpr int kRadixThreads = 256;
 constexpr int kRadixBins = 256;
 constexpr long long kRadixMaxN = (1LL << 31) - 2;  // look-back words hold prefix + 1 in 31 bits

@@ -36,6 +36,7 @@
 #include <cuda_runtime.h>
 
 #include <cuda/atomic>
+#include <type_traits>
 
 #include "turtle_device.cuh"
 #include "turtle_internal.h"
@@ -46,7 +47,10 @@ namespace {
 constexpr unsigned kRFull = 0xffffffffu;
 constexpr unsigned kLbInclusive = 0x80000000u;  // word holds the inclusive prefix, else the tile's count
 constexpr int kRWarps = kRadixThreads / 32;
-static_assert(kRadixThreads == kRadixBins, "one pass thread per digit value");
+constexpr int kBinWarps = kRadixBins / 32;  // warps whose threads each own one digit value
+constexpr int kLbWindow = 4;  // look-back words loaded per round trip
+static_assert(kRadixThreads >= kRadixBins && kRadixThreads % kRadixBins == 0,
+              "threads 0..255 of a pass CTA each own one digit value");
 
 // Look-back words: 0 = not published; else flag | (value + 1).
 __device__ __forceinline__ unsigned lb_load(const unsigned* p) {
@@ -163,108 +167,127 @@ __global__ void __launch_bounds__(kRadixBins) radix_plan_kernel(SortArgs a) {
   }
 }
 
-// One pass over digit p (bits 8p .. 8p+7 of the unsigned key image).  With
-// ids a thread holds 2 x kItems loaded words: three resident CTAs per SM
-// leave it enough registers.
-//
-// Order of work in a tile: load; count the tile's digit values (shared
-// atomics) and publish the counts at once, so later tiles can add them; rank
-// and scan (no other tile needed); look back and publish the inclusive prefix;
-// stage and write.  Measured on 2^26 int32 keys + ids: 1.88 ms in this order,
-// 1.99 ms when the look-back runs before the ranking (with or without its
-// first loads issued early), 2.53 ms when the counts are published only after
-// the ranking.
+// Digit p (byte p) of an unsigned key image: one byte-permute for 32-bit
+// words.
+template <typename KT>
+__device__ __forceinline__ unsigned digit_of(KT k, int p) {
+  if constexpr (sizeof(KT) == 8) {
+    const unsigned half = p >= 4 ? (unsigned)((unsigned long long)k >> 32) : (unsigned)k;
+    return __byte_perm(half, 0u, 0x4440u | (unsigned)(p & 3));
+  } else {
+    return __byte_perm((unsigned)k, 0u, 0x4440u | (unsigned)p);
+  }
+}
+
+// The same digit through an opaque byte-permute: keeps the compiler from
+// holding every item's digit in a register from the ranking to the staging.
+template <typename KT>
+__device__ __forceinline__ unsigned digit_again(KT k, int p) {
+  unsigned half, d;
+  if constexpr (sizeof(KT) == 8) half = p >= 4 ? (unsigned)((unsigned long long)k >> 32) : (unsigned)k;
+  else half = (unsigned)k;
+  asm volatile("prmt.b32 %0, %1, 0, %2;" : "=r"(d) : "r"(half), "r"(0x4440u | (unsigned)(p & 3)));
+  return d;
+}
+
 template <typename U, bool kIdx>
-__global__ void __launch_bounds__(kRadixThreads, kIdx ? 3 : 4) radix_pass_kernel(SortArgs a, int p) {
+struct RadixSmem {
+  static constexpr int kTile = kRadixThreads * radix_items(sizeof(U));
+  unsigned short wc[kRWarps][kRadixBins];  // warp running counts, then staging starts per warp
+  unsigned mm[kRWarps][kRadixBins];        // lanes of each digit value (one item)
+  unsigned cnt[kRadixBins];                // the tile's count of each digit value, then its
+                                           // first staging slot of each value
+  int dst[kRadixBins];                     // the pass's first output position of each value,
+                                           // then the output position of staging slot 0
+  unsigned wsum[kBinWarps];
+  int tile, fail;
+  U k[kTile];                              // the tile in digit order
+  int i[kIdx ? kTile : 1];
+};
+
+// The work of one tile (`valid` keys; kFull: all kTile).  Order: load; count
+// the tile's digit values (shared atomics) and publish the counts at once, so
+// later tiles can add them; rank (no other tile needed); look back and publish
+// the inclusive prefix; stage and write.  Measured on 2^26 int32 keys + ids:
+// 1.88 ms in this order, 1.99 ms when the look-back runs before the ranking
+// (with or without its first loads issued early), 2.53 ms when the counts are
+// published only after the ranking.
+template <typename U, bool kIdx, bool kFull>
+__device__ __forceinline__ void radix_pass_tile(const SortArgs& a, int p, int ord, bool lastPass,
+                                           RadixSmem<U, kIdx>& sm, int tile, int valid) {
   using KT = typename KeyCfg<U>::KT;
   constexpr int kItems = radix_items(sizeof(U));
   constexpr int kTile = kRadixThreads * kItems;
-  static_assert(kTile <= 65535, "per-warp counts and offsets are 16-bit");
-  __shared__ int s_tile;
-  __shared__ int s_fail;
-  __shared__ unsigned short s_wc[kRWarps][kRadixBins];  // warp running counts, then warp offsets
-  __shared__ unsigned s_mm[kRWarps][kRadixBins];        // lanes of each digit value (one item)
-  __shared__ unsigned s_cnt[kRadixBins];                // the tile's count of each digit value
-  __shared__ int s_start[kRadixBins];                   // first staging slot of each digit value
-  __shared__ int s_dst[kRadixBins];                     // output position of staging slot 0, per value
-  __shared__ unsigned s_wsum[kRWarps];
-  __shared__ U s_k[kTile];
-  __shared__ int s_i[kIdx ? kTile : 1];
-
-  const RadixCtl* c = a.radixCtl;
-  const int ord = c->ord[p];
-  if (ord < 0) return;  // every key has the same digit: nothing moves
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const bool lastPass = p == c->last;
+  const int b = tid;  // threads b < 256: the digit value they publish, scan and look back for
+  const bool binT = b < kRadixBins;
   const bool fromB = (ord & 1) != 0;
-  const U* srcK = (const U*)(fromB ? a.keysB : a.keysA);
-  U* dstK = (U*)(fromB ? a.keysA : a.keysB);
-  const int* srcI = fromB ? a.idxB : a.idxA;
-  int* dstI = fromB ? a.idxA : a.idxB;
-  const long long n = a.n;
-  const long long tiles = (n + kTile - 1) / kTile;
-  unsigned* own = a.radixStatus + (size_t)(ord & 1) * a.radixTiles * kRadixBins;
-  unsigned* other = a.radixStatus + (size_t)((ord & 1) ^ 1) * a.radixTiles * kRadixBins;
-
-  if (tid == 0) {
-    s_tile = (int)atomicAdd(&a.radixCtl->tileCtr[p], 1u);
-    s_fail = 0;
-  }
-  for (int i = lane; i < kRadixBins; i += 32) {
-    s_wc[warp][i] = 0;
-    s_mm[warp][i] = 0u;
-  }
-  s_cnt[tid] = 0u;
-  __syncthreads();
-  const int tile = s_tile;
-  if (tile >= tiles) return;  // the grid is exactly `tiles` CTAs
-  const int b = tid;  // the digit value this thread counts, scans and looks back for
-  const unsigned gbase = a.radixBase[p * kRadixBins + b];
-  // the next moving pass uses the other region: clear this tile's row of it
-  // (the pass that used it last has finished)
-  other[(size_t)tile * kRadixBins + tid] = 0u;
-
   const KT flip = (KT)a.flip;
-  const int shift = 8 * p;
-  // warp-striped items: item i of this lane is tile element w*32*kItems + 32i + lane
-  const long long e0 = (long long)tile * kTile + (long long)warp * 32 * kItems + lane;
+  // warp-striped items: item i of this lane is tile element e0 + 32 i
+  const int e0 = warp * 32 * kItems + lane;
+  unsigned okm = (1u << kItems) - 1u;
+  if (!kFull) {
+    okm = 0u;
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) okm |= (e0 + 32 * i < valid ? 1u : 0u) << i;
+  }
   KT key[kItems];
   int id[kIdx ? kItems : 1];
+  {
+    const long long tbase = (long long)tile * kTile;
+    const U* tk = (const U*)(fromB ? a.keysB : a.keysA) + tbase;
+    const int* ti = kIdx ? (fromB ? a.idxB : a.idxA) + tbase : nullptr;
 #pragma unroll
-  for (int i = 0; i < kItems; ++i) {
-    const long long e = e0 + 32 * i;
-    const bool ok = e < n;
-    key[i] = ok ? KT(__ldcs(srcK + e)) ^ flip : KT(0);
-    if (kIdx) id[i] = ok ? __ldcs(srcI + e) : 0;
+    for (int i = 0; i < kItems; ++i) {
+      const bool ok = kFull || ((okm >> i) & 1u);
+      key[i] = ok ? KT(__ldcs(tk + e0 + 32 * i)) ^ flip : KT(0);
+      if (kIdx) id[i] = ok ? __ldcs(ti + e0 + 32 * i) : 0;
+    }
   }
-  // 1. the tile's digit counts, published at once
+  // 1. the tile's digit counts, published at once; the tile's staging start
+  // of each digit value (exclusive prefix over the values)
 #pragma unroll
   for (int i = 0; i < kItems; ++i)
-    if (e0 + 32 * i < n) atomicAdd(&s_cnt[(unsigned)(key[i] >> shift) & 255u], 1u);
+    if (kFull || ((okm >> i) & 1u)) atomicAdd(&sm.cnt[digit_of<KT>(key[i], p)], 1u);
   __syncthreads();
-  const unsigned cnt = s_cnt[b];
-  unsigned* row = own + (size_t)tile * kRadixBins;
+  const unsigned cnt = binT ? sm.cnt[b] : 0u;
   const bool mute = a.radixStall == (long long)tile + 1;  // testing: later tiles wait in vain
-  if (!mute) lb_store(&row[b], (tile == 0 ? kLbInclusive : 0u) | (cnt + 1u));
+  if (binT && !mute)
+    lb_store(a.radixStatus + ((size_t)(ord & 1) * a.radixTiles + tile) * kRadixBins + b,
+             (tile == 0 ? kLbInclusive : 0u) | (cnt + 1u));
+  {
+    unsigned x = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(kRFull, x, o);
+      if (lane >= o) x += y;
+    }
+    if (binT && lane == 31) sm.wsum[warp] = x;
+    __syncthreads();
+    if (binT) {
+      unsigned pre = 0;
+#pragma unroll
+      for (int w = 0; w < kBinWarps; ++w) pre += w < warp ? sm.wsum[w] : 0u;
+      sm.cnt[b] = pre + x - cnt;  // thread b alone reads and writes entry b
+    }
+  }
   // 2. rank: item by item in memory order (stable).  The lanes of one digit
   // value are found by each setting its bit in the warp's word for that value;
   // the warp's running count of the value is updated by the group's highest lane.
-  unsigned lt;
-  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+  const unsigned lanebit = 1u << lane, lt = lanebit - 1u;
   unsigned rk[kItems / 2];
-  unsigned short* wc = s_wc[warp];
-  unsigned* mm = s_mm[warp];
+  unsigned short* wc = sm.wc[warp];
+  unsigned* mm = sm.mm[warp];
 #pragma unroll
   for (int i = 0; i < kItems; ++i) {
-    const bool ok = e0 + 32 * i < n;
-    const unsigned d = (unsigned)(key[i] >> shift) & 255u;
-    if (ok) atomicOr(&mm[d], 1u << lane);
+    const bool ok = kFull || ((okm >> i) & 1u);
+    const unsigned d = digit_of<KT>(key[i], p);
+    if (ok) atomicOr(&mm[d], lanebit);
     __syncwarp();
-    const unsigned peers = ok ? mm[d] : 0u;
-    unsigned base = 0, r = 0;
+    unsigned peers = 0u, base = 0u;
     if (ok) {
+      peers = mm[d];
       base = wc[d];
-      r = base + __popc(peers & lt);
     }
     __syncwarp();
     if (ok && (peers >> lane) == 1u) {
@@ -272,49 +295,39 @@ __global__ void __launch_bounds__(kRadixThreads, kIdx ? 3 : 4) radix_pass_kernel
       mm[d] = 0u;
     }
     __syncwarp();
+    const unsigned r = base + __popc(peers & lt);
     if (i & 1) rk[i >> 1] |= r << 16;
     else rk[i >> 1] = r;
   }
   __syncthreads();
-  // 3. warp offsets of digit value b, and its first staging slot (exclusive
-  // prefix of the tile's counts over the digit values)
-  {
-    unsigned run = 0;
+  // 3. staging start of digit value b for each warp: the tile's start of b
+  // plus the counts of b in the warps before
+  if (binT) {
+    unsigned run = sm.cnt[b];
 #pragma unroll
     for (int w = 0; w < kRWarps; ++w) {
-      const unsigned x = s_wc[w][b];
-      s_wc[w][b] = (unsigned short)run;
+      const unsigned x = sm.wc[w][b];
+      sm.wc[w][b] = (unsigned short)run;
       run += x;
     }
-    unsigned x = cnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned y = __shfl_up_sync(kRFull, x, o);
-      if (lane >= o) x += y;
-    }
-    if (lane == 31) s_wsum[warp] = x;
-    __syncthreads();
-    unsigned pre = 0;
-#pragma unroll
-    for (int w = 0; w < kRWarps; ++w) pre += w < warp ? s_wsum[w] : 0u;
-    s_start[b] = (int)(pre + x - cnt);
   }
   // 4. decoupled look-back: add the published words of the tiles before this
-  // one, four at a time, back to the first inclusive prefix
+  // one, kLbWindow at a time, back to the first inclusive prefix
   unsigned excl = 0;
-  if (tile > 0) {
+  const unsigned* own = a.radixStatus + (size_t)(ord & 1) * a.radixTiles * kRadixBins;
+  if (binT && tile > 0) {
     const long long limit = a.barrierPolls > 0 ? a.barrierPolls : kSpinLimit;
     long long polls = 0;
     long long j = tile - 1;
     for (;;) {
-      unsigned w[4];
+      unsigned w[kLbWindow];
 #pragma unroll
-      for (int q = 0; q < 4; ++q)
+      for (int q = 0; q < kLbWindow; ++q)
         w[q] = j - q >= 0 ? lb_load(own + (size_t)(j - q) * kRadixBins + b) : (kLbInclusive | 1u);
       bool stop = false, incl = false;
       int used = 0;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
+      for (int q = 0; q < kLbWindow; ++q) {
         if (!stop) {
           if (w[q] == 0u) {
             stop = true;  // not published yet: poll it again
@@ -330,45 +343,91 @@ __global__ void __launch_bounds__(kRadixThreads, kIdx ? 3 : 4) radix_pass_kernel
       if (used == 0 &&
           (++polls > limit || ((polls & 255) == 0 && ld_acquire_int(&a.ctrl->error) != 0))) {
         set_error(a.ctrl, kDevTimeout, kSiteLookback, tile);
-        s_fail = 1;
+        sm.fail = 1;
         break;
       }
     }
-    if (!mute) lb_store(&row[b], kLbInclusive | (excl + cnt + 1u));
+    if (!mute)
+      lb_store(a.radixStatus + ((size_t)(ord & 1) * a.radixTiles + tile) * kRadixBins + b,
+               kLbInclusive | (excl + cnt + 1u));
   }
-  s_dst[b] = (int)(gbase + excl) - s_start[b];
+  if (binT) sm.dst[b] = sm.dst[b] + (int)excl - (int)sm.cnt[b];
   __syncthreads();
   // 5. stage the tile in digit order
 #pragma unroll
   for (int i = 0; i < kItems; ++i) {
-    if (e0 + 32 * i < n) {
-      const unsigned d = (unsigned)(key[i] >> shift) & 255u;
+    if (kFull || ((okm >> i) & 1u)) {
+      const unsigned d = digit_again<KT>(key[i], p);
       const unsigned r = (i & 1) ? rk[i >> 1] >> 16 : rk[i >> 1] & 0xFFFFu;
-      const int pos = s_start[d] + (int)s_wc[warp][d] + (int)r;
-      s_k[pos] = U(key[i] ^ flip);
-      if (kIdx) s_i[pos] = id[i];
+      const int pos = (int)sm.wc[warp][d] + (int)r;
+      sm.k[pos] = U(key[i] ^ flip);
+      if (kIdx) sm.i[pos] = id[i];
     }
   }
   __syncthreads();
-  if (s_fail) return;
+  if (sm.fail) return;
   // 6. write-out: thread t takes staging slots t, t + 256, ...; consecutive
   // slots of one digit value go to consecutive addresses
-  const long long left = n - (long long)tile * kTile;
-  const int valid = left < kTile ? (int)left : kTile;
+  const unsigned un = (unsigned)a.n;
+  U* dstK = (U*)(fromB ? a.keysA : a.keysB);
+  int* dstI = fromB ? a.idxA : a.idxB;
+  auto write = [&](auto unmap) {
 #pragma unroll
-  for (int i = 0; i < kItems; ++i) {
-    const int s = i * kRadixThreads + tid;
-    if (s < valid) {
-      U raw = s_k[s];
-      const unsigned d = (unsigned)((KT(raw) ^ flip) >> shift) & 255u;
-      const long long dst = (long long)s_dst[d] + s;
-      if (dst >= 0 && dst < n) {  // always, when the look-back completed
-        if (sizeof(U) >= 4 && lastPass && a.fbits != 0) raw = float_image<U>(raw, true);
-        dstK[dst] = raw;
-        if (kIdx) dstI[dst] = s_i[s];
+    for (int i = 0; i < kItems; ++i) {
+      const int sl = i * kRadixThreads + tid;
+      if (kFull || sl < valid) {
+        U raw = sm.k[sl];
+        const int dst = sm.dst[digit_of<KT>(KT(raw) ^ flip, p)] + sl;
+        if ((unsigned)dst < un) {  // always, when the look-back completed
+          if constexpr (decltype(unmap)::value) raw = float_image<U>(raw, true);
+          dstK[dst] = raw;
+          if (kIdx) dstI[dst] = sm.i[sl];
+        }
       }
     }
+  };
+  if (sizeof(U) >= 4 && lastPass && a.fbits != 0) write(std::true_type{});
+  else write(std::false_type{});
+}
+
+// One pass over digit p (bits 8p .. 8p+7 of the unsigned key image).  With
+// ids a thread holds 2 x kItems loaded words: three resident CTAs per SM
+// leave it enough registers.  The shared block (RadixSmem) is dynamic.
+template <typename U, bool kIdx>
+__global__ void __launch_bounds__(kRadixThreads, kIdx ? 3 : 4) radix_pass_kernel(SortArgs a, int p) {
+  constexpr int kTile = RadixSmem<U, kIdx>::kTile;
+  static_assert(kTile <= 65535, "per-warp counts and staging starts are 16-bit");
+  extern __shared__ __align__(16) unsigned char radix_smem[];
+  RadixSmem<U, kIdx>& sm = *reinterpret_cast<RadixSmem<U, kIdx>*>(radix_smem);
+  const RadixCtl* c = a.radixCtl;
+  const int ord = c->ord[p];
+  if (ord < 0) return;  // every key has the same digit: nothing moves
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const long long n = a.n;
+  const long long tiles = (n + kTile - 1) / kTile;
+  if (tid == 0) {
+    sm.tile = (int)atomicAdd(&a.radixCtl->tileCtr[p], 1u);
+    sm.fail = 0;
   }
+  for (int i = lane; i < kRadixBins; i += 32) {
+    sm.wc[warp][i] = 0;
+    sm.mm[warp][i] = 0u;
+  }
+  if (tid < kRadixBins) {
+    sm.cnt[tid] = 0u;
+    sm.dst[tid] = (int)a.radixBase[p * kRadixBins + tid];
+  }
+  __syncthreads();
+  const int tile = sm.tile;
+  if (tile >= tiles) return;  // the grid is exactly `tiles` CTAs
+  // the next moving pass uses the other look-back region: clear this tile's
+  // row of it (the pass that used it last has finished)
+  if (tid < kRadixBins)
+    a.radixStatus[(size_t)((ord & 1) ^ 1) * a.radixTiles * kRadixBins + (size_t)tile * kRadixBins + tid] = 0u;
+  const bool lastPass = p == c->last;
+  const long long left = n - (long long)tile * kTile;
+  if (left >= kTile) radix_pass_tile<U, kIdx, true>(a, p, ord, lastPass, sm, tile, kTile);
+  else radix_pass_tile<U, kIdx, false>(a, p, ord, lastPass, sm, tile, (int)left);
 }
 
 template <typename U, bool kIdx>
@@ -412,7 +471,12 @@ cudaError_t launch_radix(const SortArgs& a, cudaStream_t stream, cudaEvent_t mid
   radix_hist_kernel<U><<<(unsigned)(histBlocks > 0 ? histBlocks : 1), kRadixThreads, 0, stream>>>(a);
   radix_plan_kernel<U><<<1, kRadixBins, 0, stream>>>(a);
   if (passStart != nullptr && (e = cudaEventRecord(passStart, stream)) != cudaSuccess) return e;
-  for (int p = 0; p < P; ++p) radix_pass_kernel<U, kIdx><<<(unsigned)tiles, kRadixThreads, 0, stream>>>(a, p);
+  constexpr int smem = (int)sizeof(RadixSmem<U, kIdx>);
+  if ((e = cudaFuncSetAttribute(radix_pass_kernel<U, kIdx>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                smem)) != cudaSuccess)
+    return e;
+  for (int p = 0; p < P; ++p)
+    radix_pass_kernel<U, kIdx><<<(unsigned)tiles, kRadixThreads, smem, stream>>>(a, p);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (mid != nullptr && (e = cudaEventRecord(mid, stream)) != cudaSuccess) return e;
   const long long fb = (a.n + 255) / 256;
