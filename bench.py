@@ -332,8 +332,8 @@ def run_gpu(args) -> None:
         traffic, traffic_src = profile_traffic(n, "radix_pass_kernel")
         split = {"kernel_ms": kernel_ms, "passes_ms": pass_ms,
                  "histogram_and_plan_ms": setup_ms, "finish_ms": leaf_ms}
-        overlap = ("none: the radix form finishes every key in its last pass, so the "
-                   "result is copied back after the sort")
+        overlap = ("ids copy-in runs during the key passes (which carry element positions; "
+                   "one gather then maps them to ids); the keys copy-out overlaps the gather")
     else:
         # the two kernels (partition, leaf) are charged one pass each
         launch_bytes = alg_bytes / 2
@@ -368,6 +368,7 @@ def run_gpu(args) -> None:
                 "ms_per_step": 1e3 * sum(e2e_t) / len(e2e_t),
                 "ms_min_median_max": [1e3 * min(e2e_t), 1e3 * sorted(e2e_t)[len(e2e_t) // 2],
                                       1e3 * max(e2e_t)],
+                "ms_steps": [round(1e3 * t, 3) for t in e2e_t],
                 "gpu_launches_per_step": e2e_launches / len(e2e_t),
                 "overlap": overlap},
         "tuning": {"table": ts.tuning_source(),

@@ -112,6 +112,43 @@ def test_radix_float_all_equal(gpu, dtype):
     assert np.array_equal(i, np.arange(x.size, dtype=np.int32))
 
 
+@pytest.mark.parametrize("dtype", [np.int32, np.int64, np.uint16, np.float32])
+@pytest.mark.parametrize("dist", ["uniform", "equal", "top_byte", "narrow"])
+def test_radix_late_ids_start_sorting(gpu, dtype, dist):
+    """StartSorting with ids in pinned buffers (at least 4M keys): the ids'
+    copy-in overlaps the key passes, which carry positions; a gather then
+    turns positions into ids.  No, one and two moving passes (positions left
+    as the identity, odd and even pass counts) and float keys."""
+    torch = pytest.importorskip("torch")
+    n = (1 << 22) + 4321
+    if dtype == np.float32:
+        keys = make_floats(dtype, n, {"uniform": "wide", "equal": "dups", "top_byte": "dups",
+                                      "narrow": "specials"}[dist], 77)
+        if dist == "equal":
+            keys[:] = dtype(-0.75)
+    else:
+        keys = _dist(dtype, n, dist, 5150)
+    ids = dg.uniform(np.int32, n, 99)  # arbitrary ids, not positions
+    kt = torch.empty(keys.nbytes, dtype=torch.uint8, pin_memory=True)
+    it = torch.empty(n, dtype=torch.int32, pin_memory=True)
+    kb = kt.numpy().view(keys.dtype)[:n]
+    ib = it.numpy()
+    with TurtleSort(keys.dtype, n, track_index=True) as s:
+        for _ in range(2):
+            kb[:] = keys
+            ib[:] = ids
+            s.StartSorting(kb, ib)
+            s.Sync()
+            assert s.last_form == "radix"
+            if dtype == np.float32:
+                order = expected_order(keys)
+                assert np.array_equal(bits(kb), bits(keys[order]))
+            else:
+                order = np.argsort(keys, kind="stable")
+                assert np.array_equal(kb, keys[order])
+            assert np.array_equal(ib, ids[order])
+
+
 def test_radix_equals_pivot_forms(gpu):
     n = (1 << 24) + 3
     keys = dg.uniform(np.int32, n, 31337)

@@ -48,6 +48,7 @@ struct turtle_sorter {
   int device = 0;
   cudaStream_t stream = nullptr;
   DevBuffer keysA, idxA, keysB, idxB, ws, offsets;
+  DevBuffer idxC;  // late ids of StartSorting (allocated on first use)
   WsLayout lay;
   int grid[2] = {0, 0};
   turtle::Control* hctrl = nullptr;  // pinned status block
@@ -148,6 +149,7 @@ turtle::SortArgs make_args(turtle_sorter* s, void* keys, int32_t* idx, const lon
   a.leafYield = s->leafYield;
   a.barrierPolls = s->barrierPolls;
   a.radixStall = s->radixStall;
+  a.idxC = (int*)s->idxC.ptr;
   return a;
 }
 
@@ -347,6 +349,7 @@ turtle_status turtle_destroy(turtle_sorter* s) {
   turtle::vmm_free(&s->keysB);
   turtle::vmm_free(&s->idxA);
   turtle::vmm_free(&s->idxB);
+  turtle::vmm_free(&s->idxC);
   turtle::vmm_free(&s->ws);
   turtle::vmm_free(&s->offsets);
   if (s->hctrl) cudaFreeHost(s->hctrl);
@@ -361,6 +364,41 @@ int turtle_compression_ok(const turtle_sorter* s) {
   return (s && s->keysA.compressed) ? 1 : 0;
 }
 
+// StartSorting with ids in pinned host memory under the radix form: the ids'
+// host-to-device copy runs while the digit passes sort the keys with element
+// positions as payload (the ids are not needed until the end), then one
+// gather turns positions into ids; the keys' copy back overlaps the gather.
+// Stream order: keys in (stream) -> ids in (copy stream) | radix kernels ->
+// keys out (copy stream) | wait ids in -> gather -> ids out (copy stream).
+static turtle_status start_late_ids(turtle_sorter* s, void* host_keys, int32_t* host_idx,
+                                     long long n) {
+  cudaEvent_t* ev = s->sliceEv;  // keys in, ids in, keys final, ids final
+  TRY_CUDA(s, cudaMemcpyAsync(s->keysA.ptr, host_keys, (size_t)n * s->width,
+                              cudaMemcpyHostToDevice, s->stream));
+  TRY_CUDA(s, cudaEventRecord(ev[0], s->stream));
+  TRY_CUDA(s, cudaStreamWaitEvent(s->copyStream, ev[0], 0));
+  TRY_CUDA(s, cudaMemcpyAsync(s->idxC.ptr, host_idx, (size_t)n * sizeof(int32_t),
+                              cudaMemcpyHostToDevice, s->copyStream));
+  TRY_CUDA(s, cudaEventRecord(ev[1], s->copyStream));
+  turtle::SortArgs a = make_args(s, s->keysA.ptr, (int32_t*)s->idxA.ptr, nullptr, 0, n);
+  a.idsLate = 1;
+  TRY_CUDA(s, enqueue_persistent(s, a, true, s->stream));
+  TRY_CUDA(s, cudaEventRecord(ev[2], s->stream));
+  TRY_CUDA(s, cudaStreamWaitEvent(s->copyStream, ev[2], 0));
+  TRY_CUDA(s, cudaMemcpyAsync(host_keys, s->keysA.ptr, (size_t)n * s->width,
+                              cudaMemcpyDeviceToHost, s->copyStream));
+  TRY_CUDA(s, cudaStreamWaitEvent(s->stream, ev[1], 0));
+  TRY_CUDA(s, turtle::kernels_launch_radix_gather(a, s->stream));
+  s->launches.fetch_add(1);
+  TRY_CUDA(s, cudaEventRecord(ev[3], s->stream));
+  TRY_CUDA(s, cudaStreamWaitEvent(s->copyStream, ev[3], 0));
+  TRY_CUDA(s, cudaMemcpyAsync(host_idx, s->idxA.ptr, (size_t)n * sizeof(int32_t),
+                              cudaMemcpyDeviceToHost, s->copyStream));
+  s->overlapped = true;
+  s->pending = true;
+  return TURTLE_OK;
+}
+
 turtle_status turtle_start(turtle_sorter* s, void* host_keys, int32_t* host_idx, int64_t n) {
   if (!s || (!host_keys && n > 0) || n < 0) return TURTLE_ERR_INVALID_ARGUMENT;
   if (n > s->maxN) return TURTLE_ERR_TOO_LARGE;
@@ -373,6 +411,18 @@ turtle_status turtle_start(turtle_sorter* s, void* host_keys, int32_t* host_idx,
   s->hostIdx = host_idx;
   s->n = n;
   std::memset(s->hctrl, 0, sizeof(turtle::Control));
+  s->yielded = false;
+  const bool pinned = n > 0 && host_pinned(host_keys) && (!host_idx || host_pinned(host_idx));
+  if (host_idx && pinned && n >= kOverlapMinKeys &&
+      make_args(s, s->keysA.ptr, (int32_t*)s->idxA.ptr, nullptr, 0, n).radix) {
+    bool ready = s->idxC.ptr != nullptr;
+    if (!ready) {  // the ids' landing buffer, once per sorter; without it, the plain path
+      ready = turtle::vmm_alloc(&s->idxC, (size_t)s->maxN * sizeof(int32_t), s->device,
+                                s->compressRequested) == cudaSuccess;
+      cudaGetLastError();
+    }
+    if (ready) return start_late_ids(s, host_keys, host_idx, n);
+  }
   if (n > 0) {
     TRY_CUDA(s, cudaMemcpyAsync(s->keysA.ptr, host_keys, (size_t)n * s->width,
                                 cudaMemcpyHostToDevice, s->stream));
@@ -380,11 +430,7 @@ turtle_status turtle_start(turtle_sorter* s, void* host_keys, int32_t* host_idx,
       TRY_CUDA(s, cudaMemcpyAsync(s->idxA.ptr, host_idx, (size_t)n * sizeof(int32_t),
                                   cudaMemcpyHostToDevice, s->stream));
   }
-  const int slices = (n >= kOverlapMinKeys && host_pinned(host_keys) &&
-                      (!host_idx || host_pinned(host_idx)))
-                         ? turtle::kMaxSlices
-                         : 1;
-  s->yielded = false;
+  const int slices = (n >= kOverlapMinKeys && pinned) ? turtle::kMaxSlices : 1;
   st = sort_device_impl(s, s->keysA.ptr, host_idx ? (int32_t*)s->idxA.ptr : nullptr, n,
                         s->stream, slices);
   if (st != TURTLE_OK) return st;

@@ -245,6 +245,9 @@ struct SortArgs {
   RadixCtl* radixCtl;
   unsigned* radixStatus;     // [2][radixTiles][256] look-back words
   long long radixStall;      // testing: tile + 1 whose look-back words are never published (0: none)
+  int* idxC;                 // late ids (radix form): the caller's ids, gathered after the passes
+  int idsLate;               // 1: the passes carry element positions; radix_gather_kernel then
+                             // writes idxA[i] = idxC[position of i]
 };
 
 // ---- atomics / barrier ----

@@ -30,6 +30,9 @@ cudaError_t kernels_launch_radix(int width, bool hasIdx, const SortArgs& a, cuda
                                  cudaEvent_t passStart = nullptr);
 // Kernel launches of one radix-form sort of `width`-byte keys.
 int radix_launches(int width);
+// Late ids (a.idsLate): idxA[i] = idxC[position of i], after the radix kernels
+// and once the caller's ids are in idxC.
+cudaError_t kernels_launch_radix_gather(const SortArgs& a, cudaStream_t stream);
 cudaError_t kernels_launch_multisort(int width, bool hasIdx, void* keys, int* idx,
                                      long long numArrays, int arrSize, unsigned long long flip,
                                      int fbits, int geometry, cudaStream_t stream);

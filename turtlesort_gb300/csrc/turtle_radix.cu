@@ -212,9 +212,18 @@ struct RadixSmem {
 // 1.88 ms in this order, 1.99 ms when the look-back runs before the ranking
 // (with or without its first loads issued early), 2.53 ms when the counts are
 // published only after the ranking.
+// Late ids: the passes carry element positions instead of ids.  The first
+// moving pass makes them; the pass of rank k writes them to idxB when
+// active - 1 - k is even, else to idxA, so the last one leaves them in idxB
+// for the gather.
+__device__ __forceinline__ int* late_positions(const SortArgs& a, int active, int k) {
+  return ((active - 1 - k) & 1) == 0 ? a.idxB : a.idxA;
+}
+
 template <typename U, bool kIdx, bool kFull>
 __device__ __forceinline__ void radix_pass_tile(const SortArgs& a, int p, int ord, bool lastPass,
-                                           RadixSmem<U, kIdx>& sm, int tile, int valid) {
+                                                int active, RadixSmem<U, kIdx>& sm, int tile,
+                                                int valid) {
   using KT = typename KeyCfg<U>::KT;
   constexpr int kItems = radix_items(sizeof(U));
   constexpr int kTile = kRadixThreads * kItems;
@@ -236,12 +245,16 @@ __device__ __forceinline__ void radix_pass_tile(const SortArgs& a, int p, int or
   {
     const long long tbase = (long long)tile * kTile;
     const U* tk = (const U*)(fromB ? a.keysB : a.keysA) + tbase;
-    const int* ti = kIdx ? (fromB ? a.idxB : a.idxA) + tbase : nullptr;
+    // ids, or (late ids) the positions of the previous moving pass; the first
+    // moving pass makes the positions
+    const bool makePos = a.idsLate && ord == 0;
+    const int* ti = !kIdx || makePos ? nullptr
+                    : (a.idsLate ? late_positions(a, active, ord - 1) : (fromB ? a.idxB : a.idxA)) + tbase;
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
       const bool ok = kFull || ((okm >> i) & 1u);
       key[i] = ok ? KT(__ldcs(tk + e0 + 32 * i)) ^ flip : KT(0);
-      if (kIdx) id[i] = ok ? __ldcs(ti + e0 + 32 * i) : 0;
+      if (kIdx) id[i] = !ok ? 0 : makePos ? (int)(tbase + e0 + 32 * i) : __ldcs(ti + e0 + 32 * i);
     }
   }
   // 1. the tile's digit counts, published at once; the tile's staging start
@@ -370,7 +383,7 @@ __device__ __forceinline__ void radix_pass_tile(const SortArgs& a, int p, int or
   // slots of one digit value go to consecutive addresses
   const unsigned un = (unsigned)a.n;
   U* dstK = (U*)(fromB ? a.keysA : a.keysB);
-  int* dstI = fromB ? a.idxA : a.idxB;
+  int* dstI = a.idsLate ? late_positions(a, active, ord) : (fromB ? a.idxA : a.idxB);
   auto write = [&](auto unmap) {
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
@@ -425,9 +438,10 @@ __global__ void __launch_bounds__(kRadixThreads, kIdx ? 3 : 4) radix_pass_kernel
   if (tid < kRadixBins)
     a.radixStatus[(size_t)((ord & 1) ^ 1) * a.radixTiles * kRadixBins + (size_t)tile * kRadixBins + tid] = 0u;
   const bool lastPass = p == c->last;
+  const int active = c->active;
   const long long left = n - (long long)tile * kTile;
-  if (left >= kTile) radix_pass_tile<U, kIdx, true>(a, p, ord, lastPass, sm, tile, kTile);
-  else radix_pass_tile<U, kIdx, false>(a, p, ord, lastPass, sm, tile, (int)left);
+  if (left >= kTile) radix_pass_tile<U, kIdx, true>(a, p, ord, lastPass, active, sm, tile, kTile);
+  else radix_pass_tile<U, kIdx, false>(a, p, ord, lastPass, active, sm, tile, (int)left);
 }
 
 template <typename U, bool kIdx>
@@ -442,10 +456,23 @@ __global__ void __launch_bounds__(256) radix_finish_kernel(SortArgs a) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
     if (inB) {
       ka[i] = kb[i];  // the last pass already mapped float images back
-      if (kIdx) a.idxA[i] = a.idxB[i];
+      if (kIdx && !a.idsLate) a.idxA[i] = a.idxB[i];  // late ids: radix_gather_kernel
     } else {
       ka[i] = float_image<U>(ka[i], true);
     }
+  }
+}
+
+// Late ids: idxA[i] = idxC[position of the key now at i] (identity when no
+// pass moved keys).  Sequential position reads, gathered id reads.
+__global__ void __launch_bounds__(256) radix_gather_kernel(SortArgs a) {
+  const int active = a.radixCtl->active;
+  const int* pos = active > 0 ? a.idxB : nullptr;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long n = a.n;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const long long src = pos ? (long long)__ldcs(pos + i) : i;
+    a.idxA[i] = (src >= 0 && src < n) ? a.idxC[src] : 0;  // positions are always in range
   }
 }
 
@@ -492,6 +519,14 @@ cudaError_t launch_radix(const SortArgs& a, cudaStream_t stream, cudaEvent_t mid
 }  // namespace
 
 int radix_launches(int width) { return width + 3; }
+
+cudaError_t kernels_launch_radix_gather(const SortArgs& a, cudaStream_t stream) {
+  if (a.n < 1 || !a.idsLate || a.idxC == nullptr) return cudaErrorInvalidValue;
+  const long long fb = (a.n + 255) / 256;
+  const long long cap = 8LL * device_sms();
+  radix_gather_kernel<<<(unsigned)(fb < cap ? fb : cap), 256, 0, stream>>>(a);
+  return cudaGetLastError();
+}
 
 cudaError_t kernels_launch_radix(int width, bool hasIdx, const SortArgs& a, cudaStream_t stream,
                                  cudaEvent_t mid, const cudaEvent_t* sliceDone,
