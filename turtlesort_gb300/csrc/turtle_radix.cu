@@ -201,8 +201,13 @@ struct RadixSmem {
                                            // then the output position of staging slot 0
   unsigned wsum[kBinWarps];
   int tile, fail;
-  U k[kTile];                              // the tile in digit order
-  int i[kIdx ? kTile : 1];
+  // the tile in digit order: (key, id) pairs for keys of up to 4 bytes with
+  // ids (one 8-byte store and load per key: 1.73 vs 1.80 ms for 2^26 int32
+  // keys + ids against separate key and id arrays), else keys and ids apart
+  static constexpr bool kPair = kIdx && sizeof(U) <= 4;
+  alignas(16) uint2 kv[kPair ? kTile : 1];
+  alignas(16) U k[kPair ? 1 : kTile];
+  int i[kIdx && !kPair ? kTile : 1];
 };
 
 // The work of one tile (`valid` keys; kFull: all kTile).  Order: load; count
@@ -373,8 +378,12 @@ __device__ __forceinline__ void radix_pass_tile(const SortArgs& a, int p, int or
       const unsigned d = digit_again<KT>(key[i], p);
       const unsigned r = (i & 1) ? rk[i >> 1] >> 16 : rk[i >> 1] & 0xFFFFu;
       const int pos = (int)sm.wc[warp][d] + (int)r;
-      sm.k[pos] = U(key[i] ^ flip);
-      if (kIdx) sm.i[pos] = id[i];
+      if constexpr (RadixSmem<U, kIdx>::kPair) {
+        sm.kv[pos] = make_uint2((unsigned)U(key[i] ^ flip), (unsigned)id[i]);
+      } else {
+        sm.k[pos] = U(key[i] ^ flip);
+        if (kIdx) sm.i[pos] = id[i];
+      }
     }
   }
   __syncthreads();
@@ -389,12 +398,21 @@ __device__ __forceinline__ void radix_pass_tile(const SortArgs& a, int p, int or
     for (int i = 0; i < kItems; ++i) {
       const int sl = i * kRadixThreads + tid;
       if (kFull || sl < valid) {
-        U raw = sm.k[sl];
+        U raw;
+        int idv = 0;
+        if constexpr (RadixSmem<U, kIdx>::kPair) {
+          const uint2 v = sm.kv[sl];
+          raw = (U)v.x;
+          idv = (int)v.y;
+        } else {
+          raw = sm.k[sl];
+          if (kIdx) idv = sm.i[sl];
+        }
         const int dst = sm.dst[digit_of<KT>(KT(raw) ^ flip, p)] + sl;
         if ((unsigned)dst < un) {  // always, when the look-back completed
           if constexpr (decltype(unmap)::value) raw = float_image<U>(raw, true);
           dstK[dst] = raw;
-          if (kIdx) dstI[dst] = sm.i[sl];
+          if (kIdx) dstI[dst] = idv;
         }
       }
     }
