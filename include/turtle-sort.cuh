@@ -164,6 +164,20 @@ struct TurtleSort {
     return s;
   }
 
+  // MultiSort with an id per key (not in the reference): hostIdx holds
+  // numArraysToSort * ArrSize int ids, permuted with the keys, stably within
+  // each array.  The sorter must track indices.
+  template <typename MType, int ArrSize, int BlockSize = 32, bool UseSharedMemory = false>
+  double MultiSort(const int numArraysToSort, MType* hostDataToSort, int* hostIdx) {
+    static_assert(std::is_same<MType, Type>::value,
+                  "MultiSort sorts the sorter's own key type (as the reference's buffers do)");
+    double s = 0.0;
+    detail::check(turtle_multisort_idx(handle, hostDataToSort, reinterpret_cast<int32_t*>(hostIdx),
+                                       (int64_t)ArrSize, (int64_t)numArraysToSort, BlockSize, &s),
+                  "MultiSort", handle);
+    return s;
+  }
+
   // Device-resident sort of n keys (and ids) already in device memory; the
   // stream is a cudaStream_t (nullptr = the sorter's own stream).
   void SortDevice(Type* dKeys, int* dIdx, int64_t n, void* stream = nullptr) {

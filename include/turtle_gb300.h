@@ -102,6 +102,14 @@ turtle_status turtle_sync(turtle_sorter* s, double* seconds);
 turtle_status turtle_multisort(turtle_sorter* s, void* host_keys, int64_t arr_size,
                                int64_t num_arrays, int block_size, double* seconds);
 
+/* MultiSort with an id per key (the reference's MultiSort has none,
+ * README.md:46): as turtle_multisort, and host_idx (num_arrays * arr_size
+ * int32) is permuted with the keys, each array's ids in the stable order of
+ * its keys.  Needs a sorter created with track_index != 0. */
+turtle_status turtle_multisort_idx(turtle_sorter* s, void* host_keys, int32_t* host_idx,
+                                   int64_t arr_size, int64_t num_arrays, int block_size,
+                                   double* seconds);
+
 /* ---- device-resident forms (no reference counterpart; new API) ---- */
 
 /* Sorts n keys (and ids) that are already in device memory, in place, on

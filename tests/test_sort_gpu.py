@@ -323,6 +323,31 @@ def test_yield_and_resume(rule, pinned):
     s.close()
 
 
+@pytest.mark.parametrize("dtype", [np.int32, np.uint16, np.int64, np.float64])
+@pytest.mark.parametrize("arr", [5, 1024, 5000])
+def test_multisort_host_with_ids(dtype, arr):
+    """The host MultiSort with an id per key (turtle_multisort_idx): each
+    array sorted, its ids permuted stably with it; arbitrary ids."""
+    num = 32 * 5
+    n = arr * num
+    if dtype == np.float64:
+        keys = np.random.default_rng(arr).standard_normal(n).round(1)
+    else:
+        keys = make_keys(dtype, n, "dups", arr + 7)
+    ids = np.random.default_rng(arr + 1).integers(-2**31, 2**31 - 1, n).astype(np.int32)
+    with TurtleSort(dtype, n, track_index=True) as s:
+        k, i = keys.copy(), ids.copy()
+        secs = s.MultiSort(arr, num, k, block_size=32, index=i)
+        assert secs > 0
+        with pytest.raises(ValueError):
+            s.MultiSort(arr, num, k, index=i[:-1])
+    rows, irows = keys.reshape(num, arr), ids.reshape(num, arr)
+    for r in range(num):
+        order = np.argsort(rows[r], kind="stable")
+        assert np.array_equal(k.reshape(num, arr)[r], rows[r][order])
+        assert np.array_equal(i.reshape(num, arr)[r], irows[r][order])
+
+
 @pytest.mark.parametrize("dtype", [np.int32, np.uint8, np.int64, np.float32])
 @pytest.mark.parametrize("arr", [7, 100, 2038, 9000])
 def test_multisort_device_with_ids(dtype, arr):

@@ -156,16 +156,23 @@ class TurtleSort:
         return float(secs.value)
 
     def MultiSort(self, arr_size: int, num_arrays: int, host: np.ndarray,
-                  block_size: int = 32) -> float:
+                  block_size: int = 32, index: Optional[np.ndarray] = None) -> float:
         """Sorts ``num_arrays`` contiguous arrays of ``arr_size`` keys in place
-        (MultiSort<Type, arrSize, blockSize>, turtle-sort.cuh:265-276)."""
+        (MultiSort<Type, arrSize, blockSize>, turtle-sort.cuh:265-276).  With
+        ``index`` (int32, one per key; a sorter made with track_index) the ids
+        are permuted with the keys, stably within each array."""
         if host.dtype != self.dtype or not host.flags.c_contiguous:
             raise TypeError(f"host must be a contiguous {self.dtype} array")
         if host.size < arr_size * num_arrays:
             raise ValueError("host array smaller than num_arrays * arr_size")
+        if index is not None and (index.dtype != np.int32 or not index.flags.c_contiguous or
+                                  index.size < arr_size * num_arrays):
+            raise ValueError("index must be a contiguous int32 array with one id per key")
         secs = C.c_double(0.0)
-        st = self._lib.turtle_multisort(self._h, host.ctypes.data_as(C.c_void_p), int(arr_size),
-                                        int(num_arrays), int(block_size), C.byref(secs))
+        st = self._lib.turtle_multisort_idx(
+            self._h, host.ctypes.data_as(C.c_void_p),
+            index.ctypes.data_as(C.c_void_p) if index is not None else None, int(arr_size),
+            int(num_arrays), int(block_size), C.byref(secs))
         _check(st, "MultiSort", self._h)
         return float(secs.value)
 

@@ -39,6 +39,7 @@ SIGNATURES = [
     ("turtle_start", _I, [_P, _P, _P, _I64]),
     ("turtle_sync", _I, [_P, C.POINTER(C.c_double)]),
     ("turtle_multisort", _I, [_P, _P, _I64, _I64, _I, C.POINTER(C.c_double)]),
+    ("turtle_multisort_idx", _I, [_P, _P, _P, _I64, _I64, _I, C.POINTER(C.c_double)]),
     ("turtle_sort_device", _I, [_P, _P, _P, _I64, _P]),
     ("turtle_sort_batched_device", _I, [_P, _P, _P, _P, _I64, _I64, _P]),
     ("turtle_multisort_device", _I, [_P, _P, _P, _I64, _I64, _P]),

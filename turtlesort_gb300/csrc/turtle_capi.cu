@@ -515,22 +515,32 @@ turtle_status turtle_multisort_device(turtle_sorter* s, void* d_keys, int32_t* d
                                     arr_size * num_arrays, stream);
 }
 
-turtle_status turtle_multisort(turtle_sorter* s, void* host_keys, int64_t arr_size,
-                               int64_t num_arrays, int block_size, double* seconds) {
+turtle_status turtle_multisort_idx(turtle_sorter* s, void* host_keys, int32_t* host_idx,
+                                   int64_t arr_size, int64_t num_arrays, int block_size,
+                                   double* seconds) {
   if (!s || arr_size < 0 || num_arrays < 0 || (!host_keys && arr_size * num_arrays > 0))
     return TURTLE_ERR_INVALID_ARGUMENT;
+  turtle_status st = check_idx(s, host_idx);
+  if (st != TURTLE_OK) return st;
   if (block_size > 0 && num_arrays % block_size != 0) return TURTLE_ERR_INVALID_ARGUMENT;
   if (arr_size > 0 && num_arrays > s->maxN / arr_size) return TURTLE_ERR_TOO_LARGE;
   if (s->pending) return TURTLE_ERR_STATE;
   cudaSetDevice(s->device);
   const auto t0 = std::chrono::steady_clock::now();
-  const size_t bytes = (size_t)(arr_size * num_arrays) * s->width;
+  const long long total = arr_size * num_arrays;
+  const size_t bytes = (size_t)total * s->width;
   if (bytes > 0) {
+    int32_t* dIdx = host_idx ? (int32_t*)s->idxA.ptr : nullptr;
     TRY_CUDA(s, cudaMemcpyAsync(s->keysA.ptr, host_keys, bytes, cudaMemcpyHostToDevice, s->stream));
-    turtle_status st =
-        turtle_multisort_device(s, s->keysA.ptr, nullptr, arr_size, num_arrays, s->stream);
+    if (dIdx)
+      TRY_CUDA(s, cudaMemcpyAsync(dIdx, host_idx, (size_t)total * sizeof(int32_t),
+                                  cudaMemcpyHostToDevice, s->stream));
+    st = turtle_multisort_device(s, s->keysA.ptr, dIdx, arr_size, num_arrays, s->stream);
     if (st != TURTLE_OK) return st;
     TRY_CUDA(s, cudaMemcpyAsync(host_keys, s->keysA.ptr, bytes, cudaMemcpyDeviceToHost, s->stream));
+    if (dIdx)
+      TRY_CUDA(s, cudaMemcpyAsync(host_idx, dIdx, (size_t)total * sizeof(int32_t),
+                                  cudaMemcpyDeviceToHost, s->stream));
     TRY_CUDA(s, cudaStreamSynchronize(s->stream));
     st = device_status(s);
     if (st != TURTLE_OK) return st;
@@ -538,6 +548,11 @@ turtle_status turtle_multisort(turtle_sorter* s, void* host_keys, int64_t arr_si
   const auto t1 = std::chrono::steady_clock::now();
   if (seconds) *seconds = std::chrono::duration<double>(t1 - t0).count();
   return TURTLE_OK;
+}
+
+turtle_status turtle_multisort(turtle_sorter* s, void* host_keys, int64_t arr_size,
+                               int64_t num_arrays, int block_size, double* seconds) {
+  return turtle_multisort_idx(s, host_keys, nullptr, arr_size, num_arrays, block_size, seconds);
 }
 
 turtle_status turtle_sort_device(turtle_sorter* s, void* d_keys, int32_t* d_idx, int64_t n,
