@@ -169,7 +169,7 @@ int64_t turtle_noalloc_max_elements(void);
  * requests while their device memory fits the HBM budget: the oldest waiting
  * request opens a batch and the requests of its (dtype, ids) group among the
  * next 256 waiting ones join it, in one batched persistent launch.  Up to
- * four batches are in flight: copies in and out overlap other batches'
+ * eight batches are in flight: copies in and out overlap other batches'
  * sorts, and two batches sort at once, each on half of the GPU.  Results are
  * identical to sorting each request alone. */
 typedef struct turtle_server turtle_server; /* opaque */

@@ -156,7 +156,8 @@ turtle::SortArgs make_args(turtle_sorter* s, void* keys, int32_t* idx, const lon
 // Enqueue: reset the control block, run the persistent kernel, copy the
 // control block to the pinned status block.
 cudaError_t enqueue_persistent(turtle_sorter* s, const turtle::SortArgs& a, bool hasIdx,
-                               cudaStream_t st, bool allowTiming = true) {
+                               cudaStream_t st, bool allowTiming = true,
+                               const cudaEvent_t* keysReady = nullptr, int keyChunks = 0) {
   if (!a.resume) {
     cudaError_t e = cudaMemsetAsync(a.ctrl, 0, sizeof(turtle::Control), st);
     if (e != cudaSuccess) return e;
@@ -170,7 +171,7 @@ cudaError_t enqueue_persistent(turtle_sorter* s, const turtle::SortArgs& a, bool
   e = turtle::kernels_launch_persistent(s->width, hasIdx, a, grid > 0 ? grid : 1, st,
                                         timing ? ev[1] : nullptr,
                                         a.slices > 1 ? s->sliceEv : nullptr,
-                                        timing ? ev[3] : nullptr);
+                                        timing ? ev[3] : nullptr, keysReady, keyChunks);
   if (e != cudaSuccess) return e;
   if (timing) {
     if ((e = cudaEventRecord(ev[2], st)) != cudaSuccess) return e;
@@ -368,30 +369,42 @@ int turtle_compression_ok(const turtle_sorter* s) {
 // host-to-device copy runs while the digit passes sort the keys with element
 // positions as payload (the ids are not needed until the end), then one
 // gather turns positions into ids; the keys' copy back overlaps the gather.
-// Stream order: keys in (stream) -> ids in (copy stream) | radix kernels ->
-// keys out (copy stream) | wait ids in -> gather -> ids out (copy stream).
+// The keys come in kKeyChunks chunks on the copy stream; the histogram of
+// each chunk runs as soon as it is in, under the copy of the next.
+// Stream order: keys in, chunk by chunk, then ids in (copy stream) |
+// histogram chunks, plan, passes, finish -> keys out (copy stream) | wait ids
+// in -> gather -> ids out (copy stream).
 static turtle_status start_late_ids(turtle_sorter* s, void* host_keys, int32_t* host_idx,
                                      long long n) {
-  cudaEvent_t* ev = s->sliceEv;  // keys in, ids in, keys final, ids final
-  TRY_CUDA(s, cudaMemcpyAsync(s->keysA.ptr, host_keys, (size_t)n * s->width,
-                              cudaMemcpyHostToDevice, s->stream));
-  TRY_CUDA(s, cudaEventRecord(ev[0], s->stream));
-  TRY_CUDA(s, cudaStreamWaitEvent(s->copyStream, ev[0], 0));
-  TRY_CUDA(s, cudaMemcpyAsync(s->idxC.ptr, host_idx, (size_t)n * sizeof(int32_t),
-                              cudaMemcpyHostToDevice, s->copyStream));
-  TRY_CUDA(s, cudaEventRecord(ev[1], s->copyStream));
-  turtle::SortArgs a = make_args(s, s->keysA.ptr, (int32_t*)s->idxA.ptr, nullptr, 0, n);
-  a.idsLate = 1;
-  TRY_CUDA(s, enqueue_persistent(s, a, true, s->stream));
-  TRY_CUDA(s, cudaEventRecord(ev[2], s->stream));
-  TRY_CUDA(s, cudaStreamWaitEvent(s->copyStream, ev[2], 0));
-  TRY_CUDA(s, cudaMemcpyAsync(host_keys, s->keysA.ptr, (size_t)n * s->width,
-                              cudaMemcpyDeviceToHost, s->copyStream));
-  TRY_CUDA(s, cudaStreamWaitEvent(s->stream, ev[1], 0));
-  TRY_CUDA(s, turtle::kernels_launch_radix_gather(a, s->stream));
-  s->launches.fetch_add(1);
+  constexpr int kKeyChunks = 4;
+  static_assert(4 + kKeyChunks <= turtle::kMaxSlices, "the slice events hold both sets");
+  cudaEvent_t* ev = s->sliceEv;  // ids in, keys final, ids final, sorter stream ready
+  cudaEvent_t* chunkEv = s->sliceEv + 4;
+  // the copy stream starts after whatever the sorter's stream holds
   TRY_CUDA(s, cudaEventRecord(ev[3], s->stream));
   TRY_CUDA(s, cudaStreamWaitEvent(s->copyStream, ev[3], 0));
+  for (int c = 0; c < kKeyChunks; ++c) {
+    const long long lo = c * n / kKeyChunks, hi = (c + 1) * n / kKeyChunks;
+    TRY_CUDA(s, cudaMemcpyAsync((char*)s->keysA.ptr + lo * s->width,
+                                (const char*)host_keys + lo * s->width, (size_t)(hi - lo) * s->width,
+                                cudaMemcpyHostToDevice, s->copyStream));
+    TRY_CUDA(s, cudaEventRecord(chunkEv[c], s->copyStream));
+  }
+  TRY_CUDA(s, cudaMemcpyAsync(s->idxC.ptr, host_idx, (size_t)n * sizeof(int32_t),
+                              cudaMemcpyHostToDevice, s->copyStream));
+  TRY_CUDA(s, cudaEventRecord(ev[0], s->copyStream));
+  turtle::SortArgs a = make_args(s, s->keysA.ptr, (int32_t*)s->idxA.ptr, nullptr, 0, n);
+  a.idsLate = 1;
+  TRY_CUDA(s, enqueue_persistent(s, a, true, s->stream, true, chunkEv, kKeyChunks));
+  TRY_CUDA(s, cudaEventRecord(ev[1], s->stream));
+  TRY_CUDA(s, cudaStreamWaitEvent(s->copyStream, ev[1], 0));
+  TRY_CUDA(s, cudaMemcpyAsync(host_keys, s->keysA.ptr, (size_t)n * s->width,
+                              cudaMemcpyDeviceToHost, s->copyStream));
+  TRY_CUDA(s, cudaStreamWaitEvent(s->stream, ev[0], 0));
+  TRY_CUDA(s, turtle::kernels_launch_radix_gather(a, s->stream));
+  s->launches.fetch_add(1);
+  TRY_CUDA(s, cudaEventRecord(ev[2], s->stream));
+  TRY_CUDA(s, cudaStreamWaitEvent(s->copyStream, ev[2], 0));
   TRY_CUDA(s, cudaMemcpyAsync(host_idx, s->idxA.ptr, (size_t)n * sizeof(int32_t),
                               cudaMemcpyDeviceToHost, s->copyStream));
   s->overlapped = true;

@@ -17,17 +17,21 @@ cudaError_t kernels_prepare(int width, bool hasIdx, int device, int* grid);
 // Partition kernel, then a.slices leaf launches; sliceDone[s] (optional) is
 // recorded after leaf launch s, when every key below slice s's end is final.
 // passStart (optional) is recorded where the partition (or the radix form's
-// digit passes) begins.
+// digit passes) begins.  keysReady (radix form, optional): the keys arrive
+// in keyChunks equal chunks, chunk c complete at event keysReady[c]; the
+// histogram of each chunk starts when it has arrived.
 cudaError_t kernels_launch_persistent(int width, bool hasIdx, const SortArgs& a, int grid,
                                       cudaStream_t stream, cudaEvent_t mid = nullptr,
                                       const cudaEvent_t* sliceDone = nullptr,
-                                      cudaEvent_t passStart = nullptr);
+                                      cudaEvent_t passStart = nullptr,
+                                      const cudaEvent_t* keysReady = nullptr, int keyChunks = 0);
 // LSD radix form of a plain sort (a.radix == 1; turtle_radix.cu): histogram,
 // plan, one pass per key byte, finish.  Same events as the partition path;
 // every slice event is recorded at the end.
 cudaError_t kernels_launch_radix(int width, bool hasIdx, const SortArgs& a, cudaStream_t stream,
                                  cudaEvent_t mid = nullptr, const cudaEvent_t* sliceDone = nullptr,
-                                 cudaEvent_t passStart = nullptr);
+                                 cudaEvent_t passStart = nullptr,
+                                 const cudaEvent_t* keysReady = nullptr, int keyChunks = 0);
 // Kernel launches of one radix-form sort of `width`-byte keys.
 int radix_launches(int width);
 // Late ids (a.idsLate): idxA[i] = idxC[position of i], after the radix kernels

@@ -72,14 +72,17 @@ __device__ __forceinline__ U float_image(U b, bool inverse) {
 }
 
 template <typename U>
-__global__ void __launch_bounds__(kRadixThreads) radix_hist_kernel(SortArgs a) {
+// Keys [lo, hi) (the keys may arrive in chunks, one launch each); `clear`:
+// this launch also clears look-back region 0.
+__global__ void __launch_bounds__(kRadixThreads) radix_hist_kernel(SortArgs a, long long lo,
+                                                                    long long hi, int clear) {
   using KT = typename KeyCfg<U>::KT;
   constexpr int P = sizeof(U);
   __shared__ unsigned h[P * kRadixBins];
   const int tid = threadIdx.x, lane = tid & 31;
   for (int i = tid; i < P * kRadixBins; i += kRadixThreads) h[i] = 0u;
   // the first moving pass uses look-back region 0: clear its rows
-  {
+  if (clear) {
     const long long rows = (a.n + radix_tile(P) - 1) / radix_tile(P);
     const long long words = rows * kRadixBins;
     for (long long i = (long long)blockIdx.x * kRadixThreads + tid; i < words;
@@ -88,19 +91,18 @@ __global__ void __launch_bounds__(kRadixThreads) radix_hist_kernel(SortArgs a) {
   }
   __syncthreads();
   U* keys = (U*)a.keysA;
-  const long long n = a.n;
   const KT flip = (KT)a.flip;
   const bool fl = sizeof(U) >= 4 && a.fbits != 0;
   const long long step = (long long)gridDim.x * kRadixThreads * 4;
   // a warp takes 128 consecutive keys per round (four coalesced loads)
-  for (long long base = ((long long)blockIdx.x * kRadixThreads + (tid & ~31)) * 4; base < n;
+  for (long long base = lo + ((long long)blockIdx.x * kRadixThreads + (tid & ~31)) * 4; base < hi;
        base += step) {
     KT k[4];
     bool ok[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const long long e = base + 32 * q + lane;
-      ok[q] = e < n;
+      ok[q] = e < hi;
       U raw = ok[q] ? keys[e] : U(0);
       if (fl && ok[q]) {
         raw = float_image<U>(raw, false);
@@ -503,7 +505,8 @@ int device_sms() {
 
 template <typename U, bool kIdx>
 cudaError_t launch_radix(const SortArgs& a, cudaStream_t stream, cudaEvent_t mid,
-                         const cudaEvent_t* sliceDone, cudaEvent_t passStart) {
+                         const cudaEvent_t* sliceDone, cudaEvent_t passStart,
+                         const cudaEvent_t* keysReady, int keyChunks) {
   constexpr int P = sizeof(U);
   const long long tiles = (a.n + radix_tile(P) - 1) / radix_tile(P);
   if (a.n < 2) return cudaSuccess;
@@ -511,9 +514,17 @@ cudaError_t launch_radix(const SortArgs& a, cudaStream_t stream, cudaEvent_t mid
   const int sms = device_sms();
   cudaError_t e = cudaMemsetAsync(a.radixHist, 0, (size_t)P * kRadixBins * sizeof(unsigned), stream);
   if (e != cudaSuccess) return e;
-  const long long hb = (a.n + 4LL * kRadixThreads - 1) / (4LL * kRadixThreads);
-  const long long histBlocks = hb < 8LL * sms ? hb : 8LL * sms;
-  radix_hist_kernel<U><<<(unsigned)(histBlocks > 0 ? histBlocks : 1), kRadixThreads, 0, stream>>>(a);
+  // the histogram, in one launch or one per chunk of keys as the chunks arrive
+  const int chunks = keysReady != nullptr && keyChunks > 1 ? keyChunks : 1;
+  for (int c = 0; c < chunks; ++c) {
+    const long long lo = c * a.n / chunks, hi = (c + 1) * a.n / chunks;
+    if (keysReady != nullptr && (e = cudaStreamWaitEvent(stream, keysReady[c], 0)) != cudaSuccess)
+      return e;
+    const long long hb = (hi - lo + 4LL * kRadixThreads - 1) / (4LL * kRadixThreads);
+    const long long histBlocks = hb < 8LL * sms ? hb : 8LL * sms;
+    radix_hist_kernel<U><<<(unsigned)(histBlocks > 0 ? histBlocks : 1), kRadixThreads, 0, stream>>>(
+        a, lo, hi, c == 0 ? 1 : 0);
+  }
   radix_plan_kernel<U><<<1, kRadixBins, 0, stream>>>(a);
   if (passStart != nullptr && (e = cudaEventRecord(passStart, stream)) != cudaSuccess) return e;
   constexpr int smem = (int)sizeof(RadixSmem<U, kIdx>);
@@ -548,16 +559,16 @@ cudaError_t kernels_launch_radix_gather(const SortArgs& a, cudaStream_t stream) 
 
 cudaError_t kernels_launch_radix(int width, bool hasIdx, const SortArgs& a, cudaStream_t stream,
                                  cudaEvent_t mid, const cudaEvent_t* sliceDone,
-                                 cudaEvent_t passStart) {
+                                 cudaEvent_t passStart, const cudaEvent_t* keysReady,
+                                 int keyChunks) {
+#define TURTLE_RADIX_LAUNCH(UU, II) \
+  launch_radix<UU, II>(a, stream, mid, sliceDone, passStart, keysReady, keyChunks)
   switch (width) {
-    case 1: return hasIdx ? launch_radix<uint8_t, true>(a, stream, mid, sliceDone, passStart)
-                          : launch_radix<uint8_t, false>(a, stream, mid, sliceDone, passStart);
-    case 2: return hasIdx ? launch_radix<uint16_t, true>(a, stream, mid, sliceDone, passStart)
-                          : launch_radix<uint16_t, false>(a, stream, mid, sliceDone, passStart);
-    case 4: return hasIdx ? launch_radix<uint32_t, true>(a, stream, mid, sliceDone, passStart)
-                          : launch_radix<uint32_t, false>(a, stream, mid, sliceDone, passStart);
-    case 8: return hasIdx ? launch_radix<uint64_t, true>(a, stream, mid, sliceDone, passStart)
-                          : launch_radix<uint64_t, false>(a, stream, mid, sliceDone, passStart);
+    case 1: return hasIdx ? TURTLE_RADIX_LAUNCH(uint8_t, true) : TURTLE_RADIX_LAUNCH(uint8_t, false);
+    case 2: return hasIdx ? TURTLE_RADIX_LAUNCH(uint16_t, true) : TURTLE_RADIX_LAUNCH(uint16_t, false);
+    case 4: return hasIdx ? TURTLE_RADIX_LAUNCH(uint32_t, true) : TURTLE_RADIX_LAUNCH(uint32_t, false);
+    case 8: return hasIdx ? TURTLE_RADIX_LAUNCH(uint64_t, true) : TURTLE_RADIX_LAUNCH(uint64_t, false);
+#undef TURTLE_RADIX_LAUNCH
     default: return cudaErrorInvalidValue;
   }
 }

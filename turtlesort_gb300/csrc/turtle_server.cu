@@ -41,7 +41,7 @@
 
 namespace {
 
-constexpr int kSlots = 4;        // batches in flight
+constexpr int kSlots = 8;        // batches in flight
 constexpr int kSortStreams = 2;  // batches sorting at once
 constexpr int kWindow = 256;     // waiting requests scanned for a batch's group
 // Requests of at least kSoloKeys keys are batches of their own: a plain sort,

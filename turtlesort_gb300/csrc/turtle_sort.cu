@@ -1790,8 +1790,11 @@ cudaError_t kernels_prepare(int width, bool hasIdx, int device, int* grid) {
 
 cudaError_t kernels_launch_persistent(int width, bool hasIdx, const SortArgs& a, int grid,
                                       cudaStream_t stream, cudaEvent_t mid,
-                                      const cudaEvent_t* sliceDone, cudaEvent_t passStart) {
-  if (a.radix) return kernels_launch_radix(width, hasIdx, a, stream, mid, sliceDone, passStart);
+                                      const cudaEvent_t* sliceDone, cudaEvent_t passStart,
+                                      const cudaEvent_t* keysReady, int keyChunks) {
+  if (a.radix)
+    return kernels_launch_radix(width, hasIdx, a, stream, mid, sliceDone, passStart, keysReady,
+                                keyChunks);
   if (passStart != nullptr) {
     const cudaError_t e = cudaEventRecord(passStart, stream);
     if (e != cudaSuccess) return e;
