@@ -168,7 +168,8 @@ int64_t turtle_noalloc_max_elements(void);
  * or without ids, from any host thread.  A scheduler thread admits waiting
  * requests while their device memory fits the HBM budget: the oldest waiting
  * request opens a batch and the requests of its (dtype, ids) group among the
- * next 256 waiting ones join it, in one batched persistent launch.  Up to
+ * next 256 waiting ones join it, in one batched persistent launch; a request
+ * of at least 2^20 keys is sorted alone, as a plain sort.  Up to
  * eight batches are in flight: copies in and out overlap other batches'
  * sorts, and two batches sort at once, each on half of the GPU.  Results are
  * identical to sorting each request alone. */
