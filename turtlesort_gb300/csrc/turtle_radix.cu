@@ -16,18 +16,20 @@
 //   radix_pass_kernel    one launch per digit, one CTA per tile of
 //                        kRadixThreads x radix_items keys, tiles claimed in
 //                        order with an atomic counter.  The CTA counts its
-//                        keys' digit values and publishes the counts, adds the
-//                        counts of the tiles before it by a decoupled
-//                        look-back over their published words, ranks its keys
-//                        by digit (per-warp running counts; the lanes of one
-//                        digit value found with shared-memory atomicOr, which
-//                        measured 2.5x faster than a match instruction on
-//                        ~30 distinct values per warp), stages the tile in
-//                        shared memory in digit order and writes it out,
-//                        consecutive keys of a digit to consecutive addresses;
+//                        keys' digit values and publishes the counts, ranks
+//                        its keys by digit (per-warp running counts; the lanes
+//                        of one digit value found with shared-memory atomicOr,
+//                        which measured 2.5x faster than a match instruction
+//                        on ~30 distinct values per warp), adds the counts of
+//                        the tiles before it by a decoupled look-back over
+//                        their published words, stages the tile in shared
+//                        memory in digit order and writes it out, consecutive
+//                        keys of a digit to consecutive addresses;
 //   radix_finish_kernel  the result back into the caller's buffer when an odd
 //                        number of passes left it in the scratch buffer (and
-//                        float keys back from their images when no pass ran).
+//                        float keys back from their images when no pass ran);
+//   radix_gather_kernel  late ids (StartSorting): the passes carried element
+//                        positions; this writes the ids in sorted order.
 //
 // Every pass reads keys + ids once and writes them once; the histogram pass
 // reads the keys once more.  A look-back wait is bounded: past the poll limit
@@ -71,9 +73,9 @@ __device__ __forceinline__ U float_image(U b, bool inverse) {
   return b ^ mask;
 }
 
-template <typename U>
 // Keys [lo, hi) (the keys may arrive in chunks, one launch each); `clear`:
 // this launch also clears look-back region 0.
+template <typename U>
 __global__ void __launch_bounds__(kRadixThreads) radix_hist_kernel(SortArgs a, long long lo,
                                                                     long long hi, int clear) {
   using KT = typename KeyCfg<U>::KT;
