@@ -117,13 +117,10 @@ __global__ void __launch_bounds__(kRadixThreads) radix_hist_kernel(SortArgs a, l
 #pragma unroll
       for (int p = 0; p < P; ++p) {
         const unsigned d = (unsigned)(k[q] >> (8 * p)) & 255u;
-        const unsigned d0 = __shfl_sync(kRFull, d, 0);
-        // sorted and narrow inputs give whole warps of one digit value
-        if (__all_sync(kRFull, ok[q] && d == d0)) {
-          if (lane == 0) atomicAdd(&h[p * kRadixBins + d], 32u);
-        } else if (ok[q]) {
-          atomicAdd(&h[p * kRadixBins + d], 1u);
-        }
+        // one shared atomic per key and digit: measured faster than first
+        // testing whether the warp's 32 keys share the value (1.675 vs
+        // 1.740 ms per 2^26 int32 + id sort; sorted input 1.646 vs 1.751 ms)
+        if (ok[q]) atomicAdd(&h[p * kRadixBins + d], 1u);
       }
     }
   }
