@@ -115,3 +115,24 @@ def test_source_string(native_lib):
     assert src
     sorts, _ = parse_table()
     assert ("tune.py" in src) == bool(sorts)
+
+
+def test_tuner_table_round_trip(tmp_path, monkeypatch):
+    """tune.py reads the compiled table (the radix-only mode re-measures only
+    the radix flags of it) and writes it back unchanged."""
+    import turtlesort_gb300.tune as tune
+    sorts, multi, src = tune.read_table()
+    assert sorts and multi and src
+    expect_sorts, expect_multi = parse_table()
+    assert [tuple(r) for r in sorts] == [tuple(r) for r in expect_sorts]
+    rows = [{"width": w, "ids": i, "n": n,
+             "best": {"form": f, "tile_shift": t, "geometry": g, "leaf_cut": c, "grid_div": d,
+                      "radix": r}}
+            for w, i, n, f, t, g, c, d, r in sorts]
+    mrows = [{"width": w, "ids": i, "arr": a, "best": g} for w, i, a, g in multi]
+    out = tmp_path / "table.inc"
+    monkeypatch.setattr(tune, "TABLE", out)
+    tune.write_table(rows, mrows, src)
+    monkeypatch.setattr(tune, "TABLE", tune.HERE / "csrc" / "turtle_tuning_table.inc")
+    text = out.read_text()
+    assert text == tune.TABLE.read_text()
