@@ -4,8 +4,8 @@ The radix form moves keys by 8-bit digits, least significant first, each
 pass a stable counting scatter; digits on which every key agrees are
 skipped.  Its output must be the stable sort, the same bytes as the pivot
 forms and as the reference (keys and ids; integer data, zero tolerance).
-The cases cover every dtype, sizes around the pass tile (4096 keys, 2048 for
-64-bit keys), inputs on which some, all or no digits are skipped (even and odd
+The cases cover every dtype, sizes around the pass tiles (4096 keys with ids,
+6144 without, 2048 for 64-bit keys), inputs on which some, all or no digits are skipped (even and odd
 numbers of moving passes: the result ends in the scratch buffer and is copied
 back), float keys in totalOrder, the device entry point, and the fallback of
 batched sorts to a pivot form.
@@ -42,7 +42,7 @@ def _check(keys, ids, k, i):
 
 @pytest.mark.parametrize("dtype", ALL_DTYPES)
 @pytest.mark.parametrize("n", [2, 3, 255, 2047, 2048, 2049, 4095, 4096, 4097, 3 * 4096 + 5,
-                               100_003, 1_048_583])
+                               6143, 6144, 6145, 3 * 6144 + 7, 100_003, 1_048_583])
 def test_radix_dtypes_and_tile_edges(gpu, dtype, n):
     keys = dg.uniform(dtype, n, 9000 + n)
     ids = np.arange(n, dtype=np.int32)[::-1].copy()

@@ -14,7 +14,8 @@
 //                        whose keys all share one value is skipped, its
 //                        scatter would be the identity;
 //   radix_pass_kernel    one launch per digit, one CTA per tile of
-//                        kRadixThreads x radix_items keys, tiles claimed in
+//                        kRadixThreads x radix_items keys (4096 with ids,
+//                        6144 without, 2048 for 64-bit keys), tiles claimed in
 //                        order with an atomic counter.  The CTA counts its
 //                        keys' digit values and publishes the counts, ranks
 //                        its keys by digit (per-warp running counts; the lanes
@@ -193,7 +194,7 @@ __device__ __forceinline__ unsigned digit_again(KT k, int p) {
 
 template <typename U, bool kIdx>
 struct RadixSmem {
-  static constexpr int kTile = kRadixThreads * radix_items(sizeof(U));
+  static constexpr int kTile = kRadixThreads * radix_items(sizeof(U), kIdx);
   unsigned short wc[kRWarps][kRadixBins];  // warp running counts, then staging starts per warp
   unsigned mm[kRWarps][kRadixBins];        // lanes of each digit value (one item)
   unsigned cnt[kRadixBins];                // the tile's count of each digit value, then its
@@ -231,7 +232,7 @@ __device__ __forceinline__ void radix_pass_tile(const SortArgs& a, int p, int or
                                                 int active, RadixSmem<U, kIdx>& sm, int tile,
                                                 int valid) {
   using KT = typename KeyCfg<U>::KT;
-  constexpr int kItems = radix_items(sizeof(U));
+  constexpr int kItems = radix_items(sizeof(U), kIdx);
   constexpr int kTile = kRadixThreads * kItems;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int b = tid;  // threads b < 256: the digit value they publish, scan and look back for
@@ -424,9 +425,11 @@ __device__ __forceinline__ void radix_pass_tile(const SortArgs& a, int p, int or
 
 // One pass over digit p (bits 8p .. 8p+7 of the unsigned key image).  With
 // ids a thread holds 2 x kItems loaded words: three resident CTAs per SM
-// leave it enough registers.  The shared block (RadixSmem) is dynamic.
+// leave it enough registers; without ids 24 keys a thread also take three
+// (four for 64-bit keys, 8 a thread).  The shared block (RadixSmem) is dynamic.
 template <typename U, bool kIdx>
-__global__ void __launch_bounds__(kRadixThreads, kIdx ? 3 : 4) radix_pass_kernel(SortArgs a, int p) {
+__global__ void __launch_bounds__(kRadixThreads, kIdx || sizeof(U) != 8 ? 3 : 4)
+    radix_pass_kernel(SortArgs a, int p) {
   constexpr int kTile = RadixSmem<U, kIdx>::kTile;
   static_assert(kTile <= 65535, "per-warp counts and staging starts are 16-bit");
   extern __shared__ __align__(16) unsigned char radix_smem[];
@@ -530,8 +533,12 @@ cudaError_t launch_radix(const SortArgs& a, cudaStream_t stream, cudaEvent_t mid
   if ((e = cudaFuncSetAttribute(radix_pass_kernel<U, kIdx>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 smem)) != cudaSuccess)
     return e;
+  // the pass grid: one CTA per tile of this pass (no larger than `tiles`,
+  // counted in the smallest tile)
+  constexpr int kPassTile = RadixSmem<U, kIdx>::kTile;
+  const long long passTiles = (a.n + kPassTile - 1) / kPassTile;
   for (int p = 0; p < P; ++p)
-    radix_pass_kernel<U, kIdx><<<(unsigned)tiles, kRadixThreads, smem, stream>>>(a, p);
+    radix_pass_kernel<U, kIdx><<<(unsigned)passTiles, kRadixThreads, smem, stream>>>(a, p);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (mid != nullptr && (e = cudaEventRecord(mid, stream)) != cudaSuccess) return e;
   const long long fb = (a.n + 255) / 256;
