@@ -151,9 +151,8 @@ turtle_status turtle_stream_status(turtle_sorter* s, void* stream);
  * (1,048,576), else TURTLE_ERR_TOO_LARGE; pointers must be 16-byte aligned.
  * All calls share the scratch array: calls whose work overlaps on the GPU
  * race and corrupt each other.  The first call on a device looks up the
- * array's address and prepares the kernels; make it before any stream
- * capture.  Waits for `stream` and returns the device-side status.  Calls no
- * allocating routine. */
+ * array's address and prepares the kernels.  Waits for `stream` and returns
+ * the device-side status.  Calls no allocating routine. */
 turtle_status turtle_sort_device_noalloc(turtle_dtype dtype, void* d_keys, int32_t* d_idx,
                                          int64_t n, void* stream);
 

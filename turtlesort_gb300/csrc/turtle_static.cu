@@ -17,8 +17,7 @@
 //     Calls whose work overlaps on the GPU (several host threads, or several
 //     streams) race on the array and corrupt each other's results;
 //   * the first call on a device resolves the array's device address with
-//     cudaGetSymbolAddress (and prepares the kernels); make that first call
-//     before any stream capture;
+//     cudaGetSymbolAddress (and prepares the kernels);
 //   * the call waits for its own stream (the status words are read with one
 //     copy ordered on that stream) and returns the device-side status;
 //   * nothing here calls cudaMalloc, cudaFree or any other allocating routine.
