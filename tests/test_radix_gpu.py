@@ -4,8 +4,8 @@ The radix form moves keys by 8-bit digits, least significant first, each
 pass a stable counting scatter; digits on which every key agrees are
 skipped.  Its output must be the stable sort, the same bytes as the pivot
 forms and as the reference (keys and ids; integer data, zero tolerance).
-The cases cover every dtype, sizes around the pass tiles (4096 keys with ids,
-6144 without, 2048 for 64-bit keys), inputs on which some, all or no digits are skipped (even and odd
+The cases cover every dtype, sizes around the pass tiles (4096 keys, 2048 for
+64-bit keys, 6144 for keys-only sorts of at least 2^24 8- to 32-bit keys), inputs on which some, all or no digits are skipped (even and odd
 numbers of moving passes: the result ends in the scratch buffer and is copied
 back), float keys in totalOrder, the device entry point, and the fallback of
 batched sorts to a pivot form.
@@ -49,6 +49,23 @@ def test_radix_dtypes_and_tile_edges(gpu, dtype, n):
     for with_ids in (True, False):
         k, i, _ = _sort_radix(keys, ids if with_ids else None)
         _check(keys, ids if with_ids else None, k, i)
+
+
+@pytest.mark.parametrize("dtype", [np.uint8, np.int16, np.int32, np.uint32, np.float32])
+@pytest.mark.parametrize("n", [(1 << 24) - 1, (1 << 24) + 3 * 6144 + 7])
+def test_radix_wide_tiles_without_ids(gpu, dtype, n):
+    """Keys-only sorts of 2^24 keys and more rank 6144-key tiles; one key
+    fewer takes the 4096-key tiles.  Both sides of the switch, ragged last
+    tiles, uniform and narrow keys (two moving passes)."""
+    if dtype == np.float32:
+        keys = make_floats(dtype, n, "wide", 61)
+        k, _, _ = _sort_radix(keys, None)
+        assert np.array_equal(bits(k), bits(keys[expected_order(keys)]))
+        return
+    for name in ("uniform", "narrow"):
+        keys = _dist(dtype, n, name, 6144)
+        k, _, _ = _sort_radix(keys, None)
+        assert np.array_equal(k, np.sort(keys, kind="stable")), name
 
 
 def _dist(dtype, n, name, seed):

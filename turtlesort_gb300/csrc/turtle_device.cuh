@@ -184,22 +184,25 @@ struct Control {
 
 // ---- LSD radix form (turtle_radix.cu) ----
 // One pass per 8-bit digit; a pass CTA of kRadixThreads threads ranks a tile
-// of kRadixThreads x radix_items(width, ids) keys: 4096 with ids, 6144
-// without, 2048 for 64-bit keys.  Measured on 2^26 int32 keys + ids: 1.76 ms
-// with 256 x 16, 2.12 ms with 512 x 8 (more resident warps, but longer CTA
-// barriers and half the threads idle in the per-digit steps); 256 x 12:
-// 1.835 vs 1.669 ms; 256 x 24: 1.70 vs 1.67 ms (0.198 vs 0.172 ms at 2^22).
-// Without ids 256 x 24 wins: 1.207 vs 1.305 ms for 2^26 uint32 keys, 0.396
-// vs 0.425 ms for uint8.
+// of kRadixThreads x radix_items(width) keys (4096, or 2048 for 64-bit keys).
+// Measured on 2^26 int32 keys + ids: 1.76 ms with 256 x 16, 2.12 ms with
+// 512 x 8 (more resident warps, but longer CTA barriers and half the threads
+// idle in the per-digit steps); 256 x 12: 1.835 vs 1.669 ms; 256 x 24: 1.70
+// vs 1.67 ms (0.198 vs 0.172 ms at 2^22).
+// Large sorts of 8- to 32-bit keys without ids take kRadixWideItems keys a
+// thread (6144-key tiles): 1.207 vs 1.305 ms for 2^26 uint32 keys, 0.396 vs
+// 0.425 ms for uint8.  Below kRadixWideMinKeys (fewer tiles than a few waves
+// of resident CTAs) the longer tiles were not measured to pay, and the
+// 4096-key tiles stay.
 constexpr int kRadixThreads = 256;
 constexpr int kRadixBins = 256;
 constexpr long long kRadixMaxN = (1LL << 31) - 2;  // look-back words hold prefix + 1 in 31 bits
-__host__ __device__ constexpr int radix_items(int width, bool ids) {
-  return width == 8 ? 8 : ids ? 16 : 24;
-}
-// The smallest pass tile of a key width (the one with ids): look-back rows
-// are sized and cleared for this many tiles, an upper bound for both passes.
-__host__ __device__ constexpr int radix_tile(int width) { return kRadixThreads * radix_items(width, true); }
+constexpr int kRadixWideItems = 24;
+constexpr long long kRadixWideMinKeys = 1LL << 24;
+__host__ __device__ constexpr int radix_items(int width) { return width == 8 ? 8 : 16; }
+// The smallest pass tile of a key width: look-back rows are sized and
+// cleared for this many tiles, an upper bound for every pass.
+__host__ __device__ constexpr int radix_tile(int width) { return kRadixThreads * radix_items(width); }
 
 struct RadixCtl {
   int ord[8];            // rank of digit p among the digits that move keys (-1: skipped)

@@ -14,8 +14,9 @@
 //                        whose keys all share one value is skipped, its
 //                        scatter would be the identity;
 //   radix_pass_kernel    one launch per digit, one CTA per tile of
-//                        kRadixThreads x radix_items keys (4096 with ids,
-//                        6144 without, 2048 for 64-bit keys), tiles claimed in
+//                        kRadixThreads x radix_items keys (4096, 2048 for
+//                        64-bit keys; 6144 for large sorts of 8- to 32-bit
+//                        keys without ids), tiles claimed in
 //                        order with an atomic counter.  The CTA counts its
 //                        keys' digit values and publishes the counts, ranks
 //                        its keys by digit (per-warp running counts; the lanes
@@ -192,9 +193,9 @@ __device__ __forceinline__ unsigned digit_again(KT k, int p) {
   return d;
 }
 
-template <typename U, bool kIdx>
+template <typename U, bool kIdx, int kItems>
 struct RadixSmem {
-  static constexpr int kTile = kRadixThreads * radix_items(sizeof(U), kIdx);
+  static constexpr int kTile = kRadixThreads * kItems;
   unsigned short wc[kRWarps][kRadixBins];  // warp running counts, then staging starts per warp
   unsigned mm[kRWarps][kRadixBins];        // lanes of each digit value (one item)
   unsigned cnt[kRadixBins];                // the tile's count of each digit value, then its
@@ -227,12 +228,11 @@ __device__ __forceinline__ int* late_positions(const SortArgs& a, int active, in
   return ((active - 1 - k) & 1) == 0 ? a.idxB : a.idxA;
 }
 
-template <typename U, bool kIdx, bool kFull>
+template <typename U, bool kIdx, int kItems, bool kFull>
 __device__ __forceinline__ void radix_pass_tile(const SortArgs& a, int p, int ord, bool lastPass,
-                                                int active, RadixSmem<U, kIdx>& sm, int tile,
-                                                int valid) {
+                                                int active, RadixSmem<U, kIdx, kItems>& sm,
+                                                int tile, int valid) {
   using KT = typename KeyCfg<U>::KT;
-  constexpr int kItems = radix_items(sizeof(U), kIdx);
   constexpr int kTile = kRadixThreads * kItems;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int b = tid;  // threads b < 256: the digit value they publish, scan and look back for
@@ -380,7 +380,7 @@ __device__ __forceinline__ void radix_pass_tile(const SortArgs& a, int p, int or
       const unsigned d = digit_again<KT>(key[i], p);
       const unsigned r = (i & 1) ? rk[i >> 1] >> 16 : rk[i >> 1] & 0xFFFFu;
       const int pos = (int)sm.wc[warp][d] + (int)r;
-      if constexpr (RadixSmem<U, kIdx>::kPair) {
+      if constexpr (RadixSmem<U, kIdx, kItems>::kPair) {
         sm.kv[pos] = make_uint2((unsigned)U(key[i] ^ flip), (unsigned)id[i]);
       } else {
         sm.k[pos] = U(key[i] ^ flip);
@@ -402,7 +402,7 @@ __device__ __forceinline__ void radix_pass_tile(const SortArgs& a, int p, int or
       if (kFull || sl < valid) {
         U raw;
         int idv = 0;
-        if constexpr (RadixSmem<U, kIdx>::kPair) {
+        if constexpr (RadixSmem<U, kIdx, kItems>::kPair) {
           const uint2 v = sm.kv[sl];
           raw = (U)v.x;
           idv = (int)v.y;
@@ -425,15 +425,15 @@ __device__ __forceinline__ void radix_pass_tile(const SortArgs& a, int p, int or
 
 // One pass over digit p (bits 8p .. 8p+7 of the unsigned key image).  With
 // ids a thread holds 2 x kItems loaded words: three resident CTAs per SM
-// leave it enough registers; without ids 24 keys a thread also take three
-// (four for 64-bit keys, 8 a thread).  The shared block (RadixSmem) is dynamic.
-template <typename U, bool kIdx>
-__global__ void __launch_bounds__(kRadixThreads, kIdx || sizeof(U) != 8 ? 3 : 4)
+// leave it enough registers; without ids 16 (or 8) keys a thread fit four,
+// kRadixWideItems keys three.  The shared block (RadixSmem) is dynamic.
+template <typename U, bool kIdx, int kItems>
+__global__ void __launch_bounds__(kRadixThreads, kIdx || kItems > 16 ? 3 : 4)
     radix_pass_kernel(SortArgs a, int p) {
-  constexpr int kTile = RadixSmem<U, kIdx>::kTile;
+  constexpr int kTile = RadixSmem<U, kIdx, kItems>::kTile;
   static_assert(kTile <= 65535, "per-warp counts and staging starts are 16-bit");
   extern __shared__ __align__(16) unsigned char radix_smem[];
-  RadixSmem<U, kIdx>& sm = *reinterpret_cast<RadixSmem<U, kIdx>*>(radix_smem);
+  RadixSmem<U, kIdx, kItems>& sm = *reinterpret_cast<RadixSmem<U, kIdx, kItems>*>(radix_smem);
   const RadixCtl* c = a.radixCtl;
   const int ord = c->ord[p];
   if (ord < 0) return;  // every key has the same digit: nothing moves
@@ -462,8 +462,10 @@ __global__ void __launch_bounds__(kRadixThreads, kIdx || sizeof(U) != 8 ? 3 : 4)
   const bool lastPass = p == c->last;
   const int active = c->active;
   const long long left = n - (long long)tile * kTile;
-  if (left >= kTile) radix_pass_tile<U, kIdx, true>(a, p, ord, lastPass, active, sm, tile, kTile);
-  else radix_pass_tile<U, kIdx, false>(a, p, ord, lastPass, active, sm, tile, (int)left);
+  if (left >= kTile)
+    radix_pass_tile<U, kIdx, kItems, true>(a, p, ord, lastPass, active, sm, tile, kTile);
+  else
+    radix_pass_tile<U, kIdx, kItems, false>(a, p, ord, lastPass, active, sm, tile, (int)left);
 }
 
 template <typename U, bool kIdx>
@@ -505,6 +507,21 @@ int device_sms() {
   return sms > 0 ? sms : 1;
 }
 
+// The P digit passes, one CTA per tile of kRadixThreads x kItems keys (no
+// more tiles than the look-back rows, which are counted in the smallest tile).
+template <typename U, bool kIdx, int kItems>
+cudaError_t launch_radix_passes(const SortArgs& a, cudaStream_t stream) {
+  using Smem = RadixSmem<U, kIdx, kItems>;
+  constexpr int smem = (int)sizeof(Smem);
+  cudaError_t e = cudaFuncSetAttribute(radix_pass_kernel<U, kIdx, kItems>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  const long long passTiles = (a.n + Smem::kTile - 1) / Smem::kTile;
+  for (int p = 0; p < (int)sizeof(U); ++p)
+    radix_pass_kernel<U, kIdx, kItems><<<(unsigned)passTiles, kRadixThreads, smem, stream>>>(a, p);
+  return cudaGetLastError();
+}
+
 template <typename U, bool kIdx>
 cudaError_t launch_radix(const SortArgs& a, cudaStream_t stream, cudaEvent_t mid,
                          const cudaEvent_t* sliceDone, cudaEvent_t passStart,
@@ -529,17 +546,11 @@ cudaError_t launch_radix(const SortArgs& a, cudaStream_t stream, cudaEvent_t mid
   }
   radix_plan_kernel<U><<<1, kRadixBins, 0, stream>>>(a);
   if (passStart != nullptr && (e = cudaEventRecord(passStart, stream)) != cudaSuccess) return e;
-  constexpr int smem = (int)sizeof(RadixSmem<U, kIdx>);
-  if ((e = cudaFuncSetAttribute(radix_pass_kernel<U, kIdx>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                smem)) != cudaSuccess)
-    return e;
-  // the pass grid: one CTA per tile of this pass (no larger than `tiles`,
-  // counted in the smallest tile)
-  constexpr int kPassTile = RadixSmem<U, kIdx>::kTile;
-  const long long passTiles = (a.n + kPassTile - 1) / kPassTile;
-  for (int p = 0; p < P; ++p)
-    radix_pass_kernel<U, kIdx><<<(unsigned)passTiles, kRadixThreads, smem, stream>>>(a, p);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  constexpr bool kWideOk = !kIdx && P <= 4;
+  e = kWideOk && a.n >= kRadixWideMinKeys
+          ? launch_radix_passes<U, kIdx, kWideOk ? kRadixWideItems : radix_items(P)>(a, stream)
+          : launch_radix_passes<U, kIdx, radix_items(P)>(a, stream);
+  if (e != cudaSuccess) return e;
   if (mid != nullptr && (e = cudaEventRecord(mid, stream)) != cudaSuccess) return e;
   const long long fb = (a.n + 255) / 256;
   radix_finish_kernel<U, kIdx><<<(unsigned)(fb < 8LL * sms ? fb : 8LL * sms), 256, 0, stream>>>(a);
